@@ -1,0 +1,41 @@
+/*
+ * poh_verify.h -- Proof-of-History chain verification in libcuda-crypt.so.
+ *
+ * Reference: src/cuda-poh-verify/poh_verify.cu:74-145 (the reference
+ * declares these in that .cu file only; the symbols are exported from its
+ * libcuda-crypt.so).
+ */
+#ifndef GB300_CRYPT_POH_VERIFY_H
+#define GB300_CRYPT_POH_VERIFY_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include <stdbool.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* hashes[32*i .. 32*i+32) <- SHA-256 applied num_hashes_arr[i] times, in
+ * place (num_hashes_arr[i] == 0 leaves the entry unchanged).  Returns 0 on
+ * success, 1 when no GPU is present (as the reference), and the cudaError_t
+ * of a failed CUDA call otherwise (the reference aborts).  The caller
+ * compares the results with its expected hashes; there is no pass/fail
+ * output.  Reference: poh_verify.cu:80-144. */
+int poh_verify_many(uint8_t* hashes, const uint64_t* num_hashes_arr, size_t num_elems,
+                    uint8_t use_non_default_stream);
+
+/* Reference: poh_verify.cu:76. */
+void poh_verify_many_set_verbose(bool val);
+
+/* ---- additions of this library (no counterpart in the reference) ------- */
+
+/* Device-pointer form: hashes (16-byte aligned) and counts already in GPU
+ * memory, enqueued on `stream` without synchronising; returns a cudaError_t. */
+int gb300_poh_verify_device(uint8_t* hashes, const uint64_t* num_hashes, uint64_t num_elems, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,42 @@
+// Launch descriptors and host-side launch functions for the device kernels.
+// Shared by the C-ABI layer (crypt_api.cu) and the kernel translation units.
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+struct CurveTables;
+
+// One batch of signatures over one contiguous device packet buffer, with the
+// reference's per-signature arrays (src/cuda-ecc-ed25519/verify.cu:240-258):
+// message length, and absolute byte offsets of the public key, signature and
+// message start inside the buffer.
+struct SigBatch {
+    const uint8_t* packets;       // device
+    uint64_t packets_len;         // bytes; reads past it are refused per item
+    const uint32_t* message_lens;
+    const uint32_t* public_key_offsets;
+    const uint32_t* signature_offsets;      // for signing: private key offsets
+    const uint32_t* message_start_offsets;
+    uint32_t n;
+    uint8_t* out;                 // verify: n verdict bytes; sign: n*64 bytes
+    const CurveTables* tables;
+};
+
+// Ed25519 verify: out[i] = 1 if signature i is valid under the reference's
+// acceptance rules, else 0.
+cudaError_t launch_ed25519_verify(const SigBatch& b, cudaStream_t s);
+
+// Ed25519 sign: out[64*i ..] = R || S.  The 64-byte private key (clamped a,
+// then the nonce prefix) sits at signature_offsets[i].
+cudaError_t launch_ed25519_sign(const SigBatch& b, cudaStream_t s);
+
+// Keypairs from 32-byte seeds (reference keypair.cu:6-16).
+cudaError_t launch_ed25519_keypair(const uint8_t* seeds, uint8_t* pk, uint8_t* sk, uint32_t n,
+                                   const CurveTables* tables, cudaStream_t s);
+
+// 0 = decodes and has order not dividing 4 (reference verify.cu:88-103).
+cudaError_t launch_check_small_order(const uint8_t* points, uint8_t* out, uint32_t n,
+                                     const CurveTables* tables, cudaStream_t s);
+
+// PoH: hashes[32*i..] <- SHA-256^num_hashes[i] (hashes[32*i..]), in place.
+cudaError_t launch_poh_verify(uint8_t* hashes, const uint64_t* num_hashes, uint64_t n, cudaStream_t s);

@@ -1,0 +1,44 @@
+// Proof-of-History chain verification kernels.
+//
+// Replaces the reference's poh_verify_kernel (src/cuda-poh-verify/
+// poh_verify.cu:12-27): one thread per entry, hash <- SHA-256(hash)
+// num_hashes[i] times, in place.  The chain state lives in eight registers
+// for the whole chain; the 32-byte entries are read and written as two
+// 16-byte vectors.
+#include <cuda_runtime.h>
+#include "kernels.h"
+#include "sha256_poh.cuh"
+
+#define POH_THREADS 64
+
+namespace {
+
+__device__ __forceinline__ uint32_t bswap(uint32_t x) { return __byte_perm(x, 0, 0x0123); }
+
+__device__ __forceinline__ void poh_chain(uint8_t* entry, uint64_t count) {
+    uint4* p = reinterpret_cast<uint4*>(entry);
+    uint4 lo = p[0], hi = p[1];
+    uint32_t w[8] = {bswap(lo.x), bswap(lo.y), bswap(lo.z), bswap(lo.w),
+                     bswap(hi.x), bswap(hi.y), bswap(hi.z), bswap(hi.w)};
+#pragma unroll 1
+    for (uint64_t k = 0; k < count; k++) poh_step(w);
+    p[0] = make_uint4(bswap(w[0]), bswap(w[1]), bswap(w[2]), bswap(w[3]));
+    p[1] = make_uint4(bswap(w[4]), bswap(w[5]), bswap(w[6]), bswap(w[7]));
+}
+
+__global__ void __launch_bounds__(POH_THREADS) poh_verify_kernel(uint8_t* hashes, const uint64_t* num_hashes,
+                                                                 uint64_t n) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    poh_chain(hashes + 32 * i, num_hashes[i]);
+}
+
+}  // namespace
+
+cudaError_t launch_poh_verify(uint8_t* hashes, const uint64_t* num_hashes, uint64_t n, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    uint64_t blocks = (n + POH_THREADS - 1) / POH_THREADS;
+    if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
+    poh_verify_kernel<<<(unsigned)blocks, POH_THREADS, 0, s>>>(hashes, num_hashes, n);
+    return cudaGetLastError();
+}

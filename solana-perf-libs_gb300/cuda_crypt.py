@@ -1,0 +1,230 @@
+"""Python binding of libcuda-crypt.so (the GB300 Ed25519 / PoH library).
+
+Mirrors the reference's C interface (src/cuda-ecc-ed25519/ed25519.h,
+src/cuda-poh-verify/poh_verify.cu) one function per export, with the same
+argument meaning, over numpy buffers; plus the device-pointer forms for
+buffers already resident on the GPU (torch tensors).  There is no CPU path:
+loading fails loudly when the library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+from typing import Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcuda-crypt.so")
+
+_u8p = ctypes.POINTER(ctypes.c_uint8)
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+
+
+class GpuElems(ctypes.Structure):
+    """gpu_Elems (reference ed25519.h:35-38)."""
+    _fields_ = [("elems", _u8p), ("num", ctypes.c_uint32)]
+
+
+def build(jobs: int = 8) -> str:
+    """Compile libcuda-crypt.so for sm_103a in place (make, parallel TUs)."""
+    subprocess.run(["make", "-s", "-C", HERE, f"-j{jobs}", "libcuda-crypt.so"], check=True)
+    return LIB_PATH
+
+
+def _p(a: np.ndarray, t):
+    return a.ctypes.data_as(t)
+
+
+@dataclass
+class SigPackets:
+    """A signature batch in the reference's layout: packets of `message_size`
+    bytes back to back (one gpu_Elems run per entry of `batches`), and four
+    uint32 arrays with one entry per signature."""
+    batches: list            # list of np.uint8 arrays, each (num * message_size,)
+    message_size: int
+    message_lens: np.ndarray
+    public_key_offsets: np.ndarray
+    signature_offsets: np.ndarray        # private-key offsets when signing
+    message_start_offsets: np.ndarray
+
+    @property
+    def total_signatures(self) -> int:
+        return int(len(self.message_lens))
+
+    @property
+    def total_packets(self) -> int:
+        return int(sum(len(b) for b in self.batches) // max(1, self.message_size))
+
+    def concatenated(self) -> np.ndarray:
+        return np.concatenate(self.batches) if len(self.batches) > 1 else self.batches[0]
+
+
+class CudaCrypt:
+    """ctypes view of libcuda-crypt.so."""
+
+    def __init__(self, path: str = LIB_PATH):
+        if not os.path.exists(path):
+            raise RuntimeError(f"libcuda-crypt.so not built ({path}); run cuda_crypt.build()")
+        self.path = path
+        L = self.lib = ctypes.CDLL(path)
+        L.ed25519_init.restype = ctypes.c_bool
+        L.ed25519_set_verbose.argtypes = [ctypes.c_bool]
+        sig_many = [ctypes.POINTER(GpuElems), ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                    _u32p, _u32p, _u32p, _u32p, _u8p, ctypes.c_uint8]
+        L.ed25519_verify_many.argtypes = sig_many
+        L.ed25519_verify_many.restype = None
+        L.ed25519_sign_many.argtypes = sig_many
+        L.ed25519_sign_many.restype = None
+        L.poh_verify_many.argtypes = [_u8p, _u64p, ctypes.c_size_t, ctypes.c_uint8]
+        L.poh_verify_many.restype = ctypes.c_int
+        L.poh_verify_many_set_verbose.argtypes = [ctypes.c_bool]
+        L.ed25519_verify.argtypes = [_u8p, _u8p, ctypes.c_uint32, _u8p]
+        L.ed25519_verify.restype = ctypes.c_int
+        L.ed25519_sign.argtypes = [_u8p, _u8p, ctypes.c_size_t, _u8p, _u8p]
+        L.ed25519_create_keypair.argtypes = [_u8p, _u8p, _u8p]
+        L.ed25519_create_seed.argtypes = [_u8p]
+        L.ed25519_get_checked_scalar.argtypes = [_u8p, _u8p]
+        L.ed25519_check_packed_ge_small_order.argtypes = [_u8p]
+        L.ed25519_license.restype = ctypes.c_char_p
+        L.cuda_host_register.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint]
+        L.cuda_host_register.restype = ctypes.c_int
+        L.cuda_host_unregister.argtypes = [ctypes.c_void_p]
+        L.cuda_host_unregister.restype = ctypes.c_int
+        L.gb300_crypt_last_error.restype = ctypes.c_int
+        dev_sig = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                   ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p]
+        L.gb300_ed25519_verify_device.argtypes = dev_sig
+        L.gb300_ed25519_sign_device.argtypes = dev_sig
+        L.gb300_ed25519_keypair_device.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_uint32, ctypes.c_void_p]
+        L.gb300_poh_verify_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p]
+        L.gb300_ed25519_create_keypairs.argtypes = [_u8p, _u8p, _u8p, ctypes.c_uint32]
+
+    # ---- reference entry points ------------------------------------------
+    def init(self) -> bool:
+        return bool(self.lib.ed25519_init())
+
+    def set_verbose(self, v: bool) -> None:
+        self.lib.ed25519_set_verbose(bool(v))
+
+    def last_error(self) -> int:
+        return int(self.lib.gb300_crypt_last_error())
+
+    def _elems(self, batches: Sequence[np.ndarray], message_size: int):
+        arr = (GpuElems * max(1, len(batches)))()
+        for i, b in enumerate(batches):
+            arr[i].elems = _p(b, _u8p)
+            arr[i].num = len(b) // message_size if message_size else 0
+        return arr
+
+    def _sig_call(self, fn, sp: SigPackets, out: np.ndarray, use_non_default_stream: int):
+        batches = [np.ascontiguousarray(b, dtype=np.uint8) for b in sp.batches]
+        arrs = [np.ascontiguousarray(a, dtype=np.uint32) for a in
+                (sp.message_lens, sp.public_key_offsets, sp.signature_offsets, sp.message_start_offsets)]
+        elems = self._elems(batches, sp.message_size)
+        total_packets = sum(len(b) // sp.message_size for b in batches) if sp.message_size else 0
+        fn(elems, len(batches), sp.message_size, total_packets, len(arrs[0]), *[_p(a, _u32p) for a in arrs],
+           _p(out, _u8p), use_non_default_stream)
+        return out
+
+    def verify_many(self, sp: SigPackets, use_non_default_stream: int = 1) -> np.ndarray:
+        out = np.zeros(sp.total_signatures, dtype=np.uint8)
+        return self._sig_call(self.lib.ed25519_verify_many, sp, out, use_non_default_stream)
+
+    def sign_many(self, sp: SigPackets, use_non_default_stream: int = 1) -> np.ndarray:
+        out = np.zeros((sp.total_signatures, 64), dtype=np.uint8)
+        return self._sig_call(self.lib.ed25519_sign_many, sp, out, use_non_default_stream)
+
+    def poh_verify_many(self, hashes: np.ndarray, num_hashes, use_non_default_stream: int = 1) -> int:
+        """In place on `hashes` (uint8, n*32), like the reference."""
+        assert hashes.dtype == np.uint8 and hashes.flags["C_CONTIGUOUS"]
+        nh = np.ascontiguousarray(num_hashes, dtype=np.uint64)
+        return int(self.lib.poh_verify_many(_p(hashes, _u8p), _p(nh, _u64p), len(nh), use_non_default_stream))
+
+    def verify(self, sig: bytes, msg: bytes, pk: bytes) -> int:
+        return int(self.lib.ed25519_verify(_buf(sig), _buf(msg), len(msg), _buf(pk)))
+
+    def sign(self, msg: bytes, pk: bytes, sk: bytes) -> bytes:
+        out = (ctypes.c_uint8 * 64)()
+        self.lib.ed25519_sign(out, _buf(msg), len(msg), _buf(pk), _buf(sk))
+        return bytes(out)
+
+    def create_keypair(self, seed: bytes):
+        pk = (ctypes.c_uint8 * 32)()
+        sk = (ctypes.c_uint8 * 64)()
+        self.lib.ed25519_create_keypair(pk, sk, _buf(seed))
+        return bytes(pk), bytes(sk)
+
+    def create_keypairs(self, seeds: np.ndarray):
+        seeds = np.ascontiguousarray(seeds, dtype=np.uint8).reshape(-1, 32)
+        n = len(seeds)
+        pk = np.zeros((n, 32), dtype=np.uint8)
+        sk = np.zeros((n, 64), dtype=np.uint8)
+        rc = self.lib.gb300_ed25519_create_keypairs(_p(seeds, _u8p), _p(pk, _u8p), _p(sk, _u8p), n)
+        if rc != 0:
+            raise RuntimeError(f"gb300_ed25519_create_keypairs failed: cudaError {rc}")
+        return pk, sk
+
+    def get_checked_scalar(self, s: bytes) -> int:
+        out = (ctypes.c_uint8 * 32)()
+        return int(self.lib.ed25519_get_checked_scalar(out, _buf(s)))
+
+    def check_packed_ge_small_order(self, p: bytes) -> int:
+        return int(self.lib.ed25519_check_packed_ge_small_order(_buf(p)))
+
+    def license(self) -> str:
+        return self.lib.ed25519_license().decode()
+
+    def host_register(self, arr: np.ndarray, flags: int = 0) -> int:
+        return int(self.lib.cuda_host_register(arr.ctypes.data, arr.nbytes, flags))
+
+    def host_unregister(self, arr: np.ndarray) -> int:
+        return int(self.lib.cuda_host_unregister(arr.ctypes.data))
+
+    # ---- device-pointer forms (torch tensors on the GPU) -------------------
+    def verify_device(self, packets, message_lens, public_key_offsets, signature_offsets, message_start_offsets,
+                      out, stream=0) -> None:
+        rc = self.lib.gb300_ed25519_verify_device(
+            packets.data_ptr(), packets.numel(), message_lens.data_ptr(), public_key_offsets.data_ptr(),
+            signature_offsets.data_ptr(), message_start_offsets.data_ptr(), message_lens.numel(),
+            out.data_ptr(), stream)
+        if rc != 0:
+            raise RuntimeError(f"gb300_ed25519_verify_device: cudaError {rc}")
+
+    def sign_device(self, packets, message_lens, public_key_offsets, private_key_offsets, message_start_offsets,
+                    out, stream=0) -> None:
+        rc = self.lib.gb300_ed25519_sign_device(
+            packets.data_ptr(), packets.numel(), message_lens.data_ptr(), public_key_offsets.data_ptr(),
+            private_key_offsets.data_ptr(), message_start_offsets.data_ptr(), message_lens.numel(),
+            out.data_ptr(), stream)
+        if rc != 0:
+            raise RuntimeError(f"gb300_ed25519_sign_device: cudaError {rc}")
+
+    def keypair_device(self, seeds, pk, sk, stream=0) -> None:
+        rc = self.lib.gb300_ed25519_keypair_device(seeds.data_ptr(), pk.data_ptr(), sk.data_ptr(),
+                                                   seeds.numel() // 32, stream)
+        if rc != 0:
+            raise RuntimeError(f"gb300_ed25519_keypair_device: cudaError {rc}")
+
+    def poh_verify_device(self, hashes, num_hashes, stream=0) -> None:
+        rc = self.lib.gb300_poh_verify_device(hashes.data_ptr(), num_hashes.data_ptr(), num_hashes.numel(), stream)
+        if rc != 0:
+            raise RuntimeError(f"gb300_poh_verify_device: cudaError {rc}")
+
+
+def _buf(b) -> ctypes.Array:
+    b = bytes(b)
+    return (ctypes.c_uint8 * max(1, len(b))).from_buffer_copy(b if b else b"\0")
+
+
+_lib = None
+
+
+def get_lib() -> CudaCrypt:
+    global _lib
+    if _lib is None:
+        _lib = CudaCrypt()
+    return _lib
