@@ -171,7 +171,7 @@ __device__ bool verify_one(const SigBatch& a, const uint32_t* sVB, uint32_t i) {
         int ci = (int)((hc >> i) & 1u);
         int cn = (i < 63) ? (int)((hc >> (i + 1)) & 1u) : 0;
         int da = nib + ci - 16 * cn;
-        int ua = da < 0 ? -da : da;
+        int ua = min(da < 0 ? -da : da, 8);      // |digit| <= 8 for h < L; clamp keeps the lookup in the table
         ge_add_cached(t, R, tab[ua], da < 0);
         if ((i & 1) == 0) {
             ge_to_p3(R, t);
@@ -181,7 +181,7 @@ __device__ bool verify_one(const SigBatch& a, const uint32_t* sVB, uint32_t i) {
             int bc = (int)((scar >> k) & 1u);
             int bn = (k < 31) ? (int)((scar >> (k + 1)) & 1u) : 0;
             int db = byte + bc - 256 * bn;
-            int ub = db < 0 ? -db : db;
+            int ub = min(db < 0 ? -db : db, VB_ENTRIES - 1);
             ge_niels nb;
             load_vb(nb, sVB, ub);
             ge_add_niels(t, R, nb, db < 0);
