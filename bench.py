@@ -1,0 +1,447 @@
+#!/usr/bin/env python3
+"""Benchmark of libcuda-crypt.so on GB300.
+
+One JSON line on rank 0.  Headline workload: Proof-of-History verification
+of 4096 entries x 12500 SHA-256 steps (poh_verify_many); a step is one pass
+over that batch.  Reported beside it (same line): Ed25519 batch verification
+of 1024 packets [sig][pubkey][64-B message] (ed25519_verify_many), a large
+verification batch that fills the GPU, and batch signing.
+
+  value     hashes/s of the kernel on inputs already resident in GPU memory
+            (CUDA events on the launching stream, L2 flushed between steps)
+  e2e       the same metric through the C ABI with host buffers: host->device
+            copy of the inputs and device->host copy of the results inside
+            the timed region
+  roofline  integer-pipe roofline: algorithmic integer ops per second over
+            the measured peak of that pipe (project microbenchmark; the
+            driver's MEASURED_PEAKS.json holds HBM and bf16 only)
+  cpu_baseline  the CPU oracle on all host cores, same workload
+
+--impl reference runs the reference's CPU implementation of the path (the
+compiled reference where it was built here, else the CPU restatement of it)
+on all host cores for the same workload and metric.
+
+Launch: python bench.py [--gpus N] [--steps K] [--warmup W]; for N > 1 under
+torchrun (one process per GPU, each running the full workload: weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "solana-perf-libs_gb300")
+for _p in (REPO, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+# one GPU per rank: the C ABI's pool spreads calls over every visible GPU,
+# so each rank sees only its own
+if "LOCAL_RANK" in os.environ and "CUDA_VISIBLE_DEVICES" not in os.environ:
+    os.environ["CUDA_VISIBLE_DEVICES"] = os.environ["LOCAL_RANK"]
+
+import numpy as np  # noqa: E402
+
+POH_OPS_PER_HASH = 1384          # ALU-pipe ops per SHA-256 compression (LOP3/SHF/IADD3 each 1)
+VERIFY_MACS = 189_460            # 32x32->64 multiply-accumulates per verify (72*1532 + 44*(1540+259))
+SIGN_MACS = 46_008               # 72*474 + 44*270
+POH_ENTRIES, POH_HASHES = 4096, 12500
+VERIFY_N = 1024
+VERIFY_BIG_N = 152 * 3 * 128 * 2  # two full waves at 3 blocks of 128 per SM
+L2_FLUSH_BYTES = 256 << 20       # > 129 MB L2
+
+
+def _metric_line_common(args, world):
+    return {"n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "data": "synthetic (seeded)"}
+
+
+# ------------------------------------------------------------------ helpers --
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, period_ms: int = 100):
+        self.period_ms = period_ms
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", str(self.period_ms)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = max(smax, float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def load_traffic():
+    p = os.path.join(REPO, "profiles", "ncu_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+# ------------------------------------------------------------- our arm -----
+
+def int_peaks(lib, torch):
+    """Measured ops/s of lop3 (ALU pipe) and mad.wide.u32 (32x32->64)."""
+    import ctypes
+    L = lib.lib
+    L.gb300_int_peak_launch.argtypes = [ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                        ctypes.c_void_p, ctypes.c_void_p]
+    sink = torch.zeros(4, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks, threads, iters = sms * 8, 256, 4096
+    res = {}
+    for kind, name in ((0, "lop3"), (1, "mad_wide"), (2, "mad_lo"), (3, "shf")):
+        best = 0.0
+        for rep in range(4):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            rc = L.gb300_int_peak_launch(kind, blocks, threads, iters, sink.data_ptr(), stream.cuda_stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            assert rc == 0, rc
+            ms = e0.elapsed_time(e1)
+            if rep:
+                best = max(best, blocks * threads * iters * 16 / (ms * 1e-3))
+        res[name] = best
+    return res
+
+
+def bench_poh(lib, torch, args, world, clocks: ClockSampler):
+    import workloads
+    h0, cnt = workloads.poh_uniform(POH_ENTRIES, POH_HASHES)
+    stream = torch.cuda.current_stream()
+    d_h0 = torch.from_numpy(h0.copy()).cuda()
+    d_h = torch.empty_like(d_h0)
+    d_c = torch.from_numpy(cnt.astype(np.int64)).cuda()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
+    total = int(cnt.sum())
+
+    def step():
+        d_h.copy_(d_h0)
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        lib.poh_verify_device(d_h, d_c, stream.cuda_stream)
+        e1.record(stream)
+        return e0, e1
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    t0 = time.perf_counter()
+    evs = [step() for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    barrier(world)
+    kern_s = sum(a.elapsed_time(b) for a, b in evs) * 1e-3
+    kern_s = max_over_ranks(kern_s, world)
+    # correctness of the timed output: the chain is deterministic, compare with the e2e path below
+    dev_out = d_h.cpu().numpy()
+
+    # e2e through the C ABI (host buffers, copies inside the timed region)
+    hbuf = np.empty(POH_ENTRIES * 32, dtype=np.uint8)
+    for _ in range(max(1, args.warmup)):
+        hbuf[:] = h0.ravel()
+        lib.poh_verify_many(hbuf, cnt)
+    barrier(world)
+    e2e_s = 0.0
+    for _ in range(args.steps):
+        hbuf[:] = h0.ravel()
+        t = time.perf_counter()
+        rc = lib.poh_verify_many(hbuf, cnt)
+        e2e_s += time.perf_counter() - t
+        assert rc == 0
+    e2e_s = max_over_ranks(e2e_s, world)
+    assert np.array_equal(hbuf.reshape(-1, 32), dev_out), "device-form and C-ABI results differ"
+    return {"total": total, "kern_s": kern_s, "wall_s": wall, "e2e_s": e2e_s, "clocks": clk, "out": dev_out,
+            "h0": h0, "cnt": cnt}
+
+
+def make_verify_data(lib, n, seed):
+    import workloads
+    sp, corrupted = workloads.verify_uniform(lib.create_keypairs, lib.sign_many, n=n, seed=seed)
+    return sp, corrupted
+
+
+def bench_verify_device(lib, torch, sp, steps, warmup):
+    stream = torch.cuda.current_stream()
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    pk = dev(sp.concatenated())
+    arrs = [dev(a.astype(np.int32)) for a in
+            (sp.message_lens, sp.public_key_offsets, sp.signature_offsets, sp.message_start_offsets)]
+    out = torch.zeros(sp.total_signatures, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
+
+    def step():
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        lib.verify_device(pk, *arrs, out, stream.cuda_stream)
+        e1.record(stream)
+        return e0, e1
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    evs = [step() for _ in range(steps)]
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in evs) * 1e-3, out.cpu().numpy()
+
+
+def bench_verify_e2e(lib, sp, steps, warmup):
+    for _ in range(warmup):
+        lib.verify_many(sp)
+    s = 0.0
+    for _ in range(steps):
+        t = time.perf_counter()
+        out = lib.verify_many(sp)
+        s += time.perf_counter() - t
+    return s, out
+
+
+def cpu_poh(h0, cnt, nthreads, sample_entries):
+    from oracle.oracle import get_oracle
+    o = get_oracle()
+    h = h0[:sample_entries]
+    c = cnt[:sample_entries]
+    t = time.perf_counter()
+    o.poh_verify_many(h, c, nthreads)
+    dt = time.perf_counter() - t
+    return float(c.sum()) / dt
+
+
+def cpu_verify(sp, nthreads, reps):
+    from oracle.oracle import get_oracle
+    o = get_oracle()
+    o.verify_packets(sp, nthreads)   # warm
+    t = time.perf_counter()
+    for _ in range(reps):
+        o.verify_packets(sp, nthreads)
+    dt = time.perf_counter() - t
+    return sp.total_signatures * reps / dt
+
+
+def run_ours(args):
+    rank, world = dist_setup()
+    import torch
+    import cuda_crypt
+    lib = cuda_crypt.get_lib()
+    if not lib.init():
+        raise RuntimeError("ed25519_init(): no usable GPU")
+    torch.cuda.set_device(0)
+    traffic = load_traffic()
+    clocks = ClockSampler()
+    peaks = int_peaks(lib, torch)
+
+    # ---- headline: PoH ----
+    poh = bench_poh(lib, torch, args, world, clocks)
+    hashes_per_step = poh["total"]
+    value = hashes_per_step * args.steps * world / poh["kern_s"]
+    ms_per_step = poh["kern_s"] / args.steps * 1e3
+    e2e_value = hashes_per_step * args.steps * world / poh["e2e_s"]
+    achieved_ops = value / world * POH_OPS_PER_HASH
+    nthreads = os.cpu_count() or 1
+
+    line = {"metric": "PoH SHA-256 hashes/s", "value": value, "unit": "hashes/s"}
+    line.update(_metric_line_common(args, world))
+    line.update({
+        "ms_per_step": ms_per_step,
+        "dtype": "u32",
+        "config": {"workload": "poh_verify_many: 4096 entries x 12500 SHA-256 steps (seeded start hashes)",
+                   "entries": POH_ENTRIES, "num_hashes": POH_HASHES, "hashes_per_step": hashes_per_step,
+                   "l2": "flushed between steps (256 MB write)", "stream": "torch current stream"},
+        "roofline": {"bound": "int_alu", "achieved": achieved_ops / 1e12, "peak": peaks["lop3"] / 1e12,
+                     "unit": "Tops/s", "frac": achieved_ops / peaks["lop3"],
+                     "traffic": traffic.get("poh_verify_kernel"),
+                     "ops_per_unit": POH_OPS_PER_HASH,
+                     "peak_source": "measured lop3.b32 throughput (gb300_int_peak_launch), 'of measured'",
+                     "parallelism_cap": "4096 chains = 128 warps on 608 SM sub-partitions"},
+        "e2e": {"value": e2e_value, "unit": "hashes/s", "h2d_bytes_per_step": POH_ENTRIES * 40,
+                "d2h_bytes_per_step": POH_ENTRIES * 32, "path": "poh_verify_many (C ABI, host buffers)"},
+        "gpu_launches": args.steps,
+        "clocks": poh["clocks"],
+        "int_peaks_tops": {k: v / 1e12 for k, v in peaks.items()},
+    })
+
+    # ---- Ed25519 verify: the 1024-packet config and a GPU-filling batch ----
+    sp, corrupted = make_verify_data(lib, VERIFY_N, seed=1)
+    vsteps = max(5, args.steps)
+    k_s, out = bench_verify_device(lib, torch, sp, vsteps, args.warmup)
+    e_s, out2 = bench_verify_e2e(lib, sp, vsteps, args.warmup)
+    assert np.array_equal(out, out2) and np.array_equal(out.astype(bool), ~corrupted)
+    big, _ = make_verify_data(lib, VERIFY_BIG_N, seed=5)
+    bk_s, bout = bench_verify_device(lib, torch, big, 3, 1)
+    v_value = VERIFY_N * vsteps / k_s
+    big_value = VERIFY_BIG_N * 3 / bk_s
+    verify = {
+        "metric": "Ed25519 verifies/s", "unit": "verifies/s",
+        "config": {"workload": "ed25519_verify_many: 1024 packets [64-B sig][32-B pubkey][64-B msg], 10% bit-flipped",
+                   "signatures": VERIFY_N},
+        "value": v_value, "ms_per_step": k_s / vsteps * 1e3,
+        "e2e": {"value": VERIFY_N * vsteps / e_s, "unit": "verifies/s",
+                "h2d_bytes_per_step": VERIFY_N * (160 + 16), "d2h_bytes_per_step": VERIFY_N,
+                "path": "ed25519_verify_many (C ABI, host buffers)"},
+        "throughput_batch": {"signatures": VERIFY_BIG_N, "value": big_value,
+                             "ms_per_launch": bk_s / 3 * 1e3},
+        "roofline": {"bound": "int_imad_wide", "achieved": big_value * VERIFY_MACS / 1e12,
+                     "peak": peaks["mad_wide"] / 1e12, "unit": "Tmac/s",
+                     "frac": big_value * VERIFY_MACS / peaks["mad_wide"],
+                     "traffic": traffic.get("ed25519_verify_kernel"), "macs_per_unit": VERIFY_MACS,
+                     "measured_on": f"{VERIFY_BIG_N}-signature batch",
+                     "peak_source": "measured mad.wide.u32 throughput (gb300_int_peak_launch), 'of measured'"},
+        "gpu_launches": vsteps,
+    }
+    # ---- CPU baselines (rank 0, N = 1) ----
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sample = POH_ENTRIES
+        line["cpu_baseline"] = {"value": cpu_poh(poh["h0"], poh["cnt"], nthreads, sample), "unit": "hashes/s",
+                                "cores": nthreads, "kind": "port",
+                                "sample": f"{sample} entries x {POH_HASHES} hashes (the full workload) on "
+                                          f"{nthreads} threads, CPU oracle (restatement of the reference)"}
+        reps = 10
+        verify["cpu_baseline"] = {"value": cpu_verify(sp, nthreads, reps), "unit": "verifies/s",
+                                  "cores": nthreads, "kind": "port",
+                                  "sample": f"{reps} x 1024 verifies on {nthreads} threads, CPU oracle"}
+    line["ed25519_verify"] = verify
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+# -------------------------------------------------------- reference arm ----
+
+def run_reference(args):
+    rank, world = dist_setup()
+    if rank != 0:
+        return
+    import workloads
+    from oracle.oracle import REF_SO, get_oracle
+    nthreads = os.cpu_count() or 1
+    h0, cnt = workloads.poh_uniform(POH_ENTRIES, POH_HASHES)
+    kind = "port"
+    runner = None
+    if os.path.exists(REF_SO):
+        # the reference's own host SHA-256 chain, threads over entries
+        from concurrent.futures import ThreadPoolExecutor
+        from oracle.oracle import RefLib
+        ref = RefLib()
+        kind = "reference"
+
+        def runner(h, c):
+            rows = [bytes(r) for r in h]
+            with ThreadPoolExecutor(nthreads) as ex:
+                list(ex.map(lambda i: ref.poh_chain(rows[i], int(c[i])), range(len(rows))))
+    else:
+        o = get_oracle()
+
+        def runner(h, c):
+            o.poh_verify_many(h, c, nthreads)
+    # bounded sample per step: 1/4 of the entries (full chain length)
+    sample = POH_ENTRIES // 4
+    hs, cs = h0[:sample], cnt[:sample]
+    for _ in range(args.warmup):
+        runner(hs[:64], cs[:64])
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        runner(hs, cs)
+    dt = time.perf_counter() - t
+    value = float(cs.sum()) * args.steps / dt
+    line = {"metric": "PoH SHA-256 hashes/s", "value": value, "unit": "hashes/s", "impl": "reference"}
+    line.update(_metric_line_common(args, 1))
+    line.update({
+        "ms_per_step": dt / args.steps * 1e3, "dtype": "u32",
+        "config": {"workload": "poh_verify_many: 4096 entries x 12500 SHA-256 steps (seeded start hashes)",
+                   "entries": POH_ENTRIES, "num_hashes": POH_HASHES},
+        "cpu_baseline": {"value": value, "unit": "hashes/s", "cores": nthreads, "kind": kind,
+                         "sample": f"{sample} entries x {POH_HASHES} hashes per step on {nthreads} threads"},
+        "e2e": {"value": value, "unit": "hashes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    })
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()
