@@ -427,6 +427,35 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_case(case: str):
+    """Small single-kernel cases for ncu captures (3 launches each)."""
+    import torch
+    import cuda_crypt
+    import workloads
+    lib = cuda_crypt.get_lib()
+    assert lib.init()
+    stream = torch.cuda.current_stream()
+    if case == "poh-small":
+        h0, cnt = workloads.poh_uniform(POH_ENTRIES, 1000)
+        d_h = torch.from_numpy(h0.copy()).cuda()
+        d_c = torch.from_numpy(cnt.astype(np.int64)).cuda()
+        for _ in range(3):
+            lib.poh_verify_device(d_h, d_c, stream.cuda_stream)
+    elif case == "verify-small":
+        sp, _ = make_verify_data(lib, 152 * 64, seed=7)
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        arrs = [dev(a.astype(np.int32)) for a in
+                (sp.message_lens, sp.public_key_offsets, sp.signature_offsets, sp.message_start_offsets)]
+        out = torch.zeros(sp.total_signatures, dtype=torch.uint8, device="cuda")
+        pk = dev(sp.concatenated())
+        for _ in range(3):
+            lib.verify_device(pk, *arrs, out, stream.cuda_stream)
+    else:
+        raise SystemExit(f"unknown case {case}")
+    torch.cuda.synchronize()
+    print("case", case, "ok")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -434,7 +463,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--case", default=None, help="run one small kernel case (for profiling) and exit")
     args = ap.parse_args()
+    if args.case:
+        run_case(args.case)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
