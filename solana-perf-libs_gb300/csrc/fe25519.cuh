@@ -13,8 +13,31 @@ struct fe {
     uint32_t v[8];
 };
 
+// Multiply and square are called, not inlined (FE_INLINE_MUL=1 inlines
+// them): a verification runs ~3,000 of them from a few dozen call sites, and
+// inlining every site made the hot loop tens of KB of code, so warps stalled
+// on instruction fetch.  Operands and results stay in registers across the
+// call (no stack frame).
+#ifndef FE_INLINE_MUL
+#define FE_INLINE_MUL 0
+#endif
+#if FE_INLINE_MUL
 __device__ __forceinline__ void fe_mul(fe& r, const fe& a, const fe& b) { fe_mul_ptx(r.v, a.v, b.v); }
 __device__ __forceinline__ void fe_sq(fe& r, const fe& a) { fe_sq_ptx(r.v, a.v); }
+#else
+static __device__ __noinline__ fe fe_mul_call(const fe a, const fe b) {
+    fe r;
+    fe_mul_ptx(r.v, a.v, b.v);
+    return r;
+}
+static __device__ __noinline__ fe fe_sq_call(const fe a) {
+    fe r;
+    fe_sq_ptx(r.v, a.v);
+    return r;
+}
+__device__ __forceinline__ void fe_mul(fe& r, const fe& a, const fe& b) { r = fe_mul_call(a, b); }
+__device__ __forceinline__ void fe_sq(fe& r, const fe& a) { r = fe_sq_call(a); }
+#endif
 __device__ __forceinline__ void fe_add(fe& r, const fe& a, const fe& b) { fe_add_ptx(r.v, a.v, b.v); }
 __device__ __forceinline__ void fe_sub(fe& r, const fe& a, const fe& b) { fe_sub_ptx(r.v, a.v, b.v); }
 

@@ -9,28 +9,44 @@
 #include "kernels.h"
 #include "sha256_poh.cuh"
 
+#ifndef POH_THREADS
 #define POH_THREADS 64
+#endif
+// How many rotations of Sigma0 / Sigma1 / each schedule sigma run on the
+// multiply pipe (see poh_step_mix).
+#ifndef POH_NS0
+#define POH_NS0 0
+#endif
+#ifndef POH_NS1
+#define POH_NS1 0
+#endif
+#ifndef POH_NSG
+#define POH_NSG 0
+#endif
 
 namespace {
 
 __device__ __forceinline__ uint32_t bswap(uint32_t x) { return __byte_perm(x, 0, 0x0123); }
 
-__device__ __forceinline__ void poh_chain(uint8_t* entry, uint64_t count) {
+__device__ __forceinline__ void poh_chain(uint8_t* entry, uint64_t count, uint32_t one) {
     uint4* p = reinterpret_cast<uint4*>(entry);
     uint4 lo = p[0], hi = p[1];
     uint32_t w[8] = {bswap(lo.x), bswap(lo.y), bswap(lo.z), bswap(lo.w),
                      bswap(hi.x), bswap(hi.y), bswap(hi.z), bswap(hi.w)};
+    const PohMul M(one);
 #pragma unroll 1
-    for (uint64_t k = 0; k < count; k++) poh_step(w);
+    for (uint64_t k = 0; k < count; k++) poh_step_mix<POH_NS0, POH_NS1, POH_NSG>(w, M);
     p[0] = make_uint4(bswap(w[0]), bswap(w[1]), bswap(w[2]), bswap(w[3]));
     p[1] = make_uint4(bswap(w[4]), bswap(w[5]), bswap(w[6]), bswap(w[7]));
 }
 
+// `one` is always 1; it arrives as a kernel argument so that the rotation
+// multipliers derived from it stay opaque to the compiler (see rotr_mul).
 __global__ void __launch_bounds__(POH_THREADS) poh_verify_kernel(uint8_t* hashes, const uint64_t* num_hashes,
-                                                                 uint64_t n) {
+                                                                 uint64_t n, uint32_t one) {
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    poh_chain(hashes + 32 * i, num_hashes[i]);
+    poh_chain(hashes + 32 * i, num_hashes[i], one);
 }
 
 }  // namespace
@@ -39,6 +55,6 @@ cudaError_t launch_poh_verify(uint8_t* hashes, const uint64_t* num_hashes, uint6
     if (n == 0) return cudaSuccess;
     uint64_t blocks = (n + POH_THREADS - 1) / POH_THREADS;
     if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
-    poh_verify_kernel<<<(unsigned)blocks, POH_THREADS, 0, s>>>(hashes, num_hashes, n);
+    poh_verify_kernel<<<(unsigned)blocks, POH_THREADS, 0, s>>>(hashes, num_hashes, n, 1u);
     return cudaGetLastError();
 }

@@ -26,8 +26,33 @@ __device__ __forceinline__ uint32_t poh_k(int t) {
     return K[t];
 }
 
+// Rotation on the multiply pipe: for m = 2^(32-n),
+//   rotr(x, n) = (x * m mod 2^32) + hi32(x * m)   (the two parts do not overlap)
+// = one mul.hi and one mad.lo.  `m` must reach the kernel as a runtime value
+// (a kernel argument) or the compiler turns the products back into shifts on
+// the ALU pipe, which is the pipe this offloads.
+__device__ __forceinline__ uint32_t rotr_mul(uint32_t x, uint32_t m) {
+    uint32_t hi, r;
+    asm("mul.hi.u32 %0, %1, %2;" : "=r"(hi) : "r"(x), "r"(m));
+    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(x), "r"(m), "r"(hi));
+    return r;
+}
+
+// Multipliers 2^(32-n) for every SHA-256 rotation, built from a runtime 1.
+struct PohMul {
+    uint32_t r2, r13, r22, r6, r11, r25, r7, r18, r17, r19;
+    __device__ explicit PohMul(uint32_t one)
+        : r2(one << 30), r13(one << 19), r22(one << 10), r6(one << 26), r11(one << 21), r25(one << 7),
+          r7(one << 25), r18(one << 14), r17(one << 15), r19(one << 13) {}
+};
+
 // w[0..7]: the 32-byte hash as big-endian words; replaced by SHA-256(w).
-__device__ __forceinline__ void poh_step(uint32_t w[8]) {
+// NS0 / NS1 of the three rotations in Sigma0 / Sigma1 of every round, and NSG
+// of the two rotations in each schedule sigma, run on the multiply pipe
+// (rotr_mul); the rest use funnel shifts on the ALU pipe.  The split
+// balances the two pipes of a warp that has its sub-partition to itself.
+template <int NS0, int NS1, int NSG>
+__device__ __forceinline__ void poh_step_mix(uint32_t w[8], const PohMul& M) {
     const uint32_t iv[8] = {0x6a09e667u, 0xbb67ae85u, 0x3c6ef372u, 0xa54ff53au,
                             0x510e527fu, 0x9b05688cu, 0x1f83d9abu, 0x5be0cd19u};
     uint32_t W[16];
@@ -45,13 +70,21 @@ __device__ __forceinline__ void poh_step(uint32_t w[8]) {
             x = W[t];
         } else {
             uint32_t w15 = W[(t - 15) & 15], w2 = W[(t - 2) & 15];
-            uint32_t s0 = POH_ROTR(w15, 7) ^ POH_ROTR(w15, 18) ^ (w15 >> 3);
-            uint32_t s1 = POH_ROTR(w2, 17) ^ POH_ROTR(w2, 19) ^ (w2 >> 10);
+            uint32_t s0 = (NSG >= 1 ? rotr_mul(w15, M.r7) : POH_ROTR(w15, 7)) ^
+                          (NSG >= 2 ? rotr_mul(w15, M.r18) : POH_ROTR(w15, 18)) ^ (w15 >> 3);
+            uint32_t s1 = (NSG >= 1 ? rotr_mul(w2, M.r17) : POH_ROTR(w2, 17)) ^
+                          (NSG >= 2 ? rotr_mul(w2, M.r19) : POH_ROTR(w2, 19)) ^ (w2 >> 10);
             x = W[t & 15] + s0 + W[(t - 7) & 15] + s1;
             W[t & 15] = x;
         }
-        uint32_t t1 = h + (POH_ROTR(e, 6) ^ POH_ROTR(e, 11) ^ POH_ROTR(e, 25)) + ((e & f) ^ (~e & g)) + poh_k(t) + x;
-        uint32_t t2 = (POH_ROTR(a, 2) ^ POH_ROTR(a, 13) ^ POH_ROTR(a, 22)) + ((a & b) | (c & (a | b)));
+        uint32_t S1 = (NS1 >= 1 ? rotr_mul(e, M.r6) : POH_ROTR(e, 6)) ^
+                      (NS1 >= 2 ? rotr_mul(e, M.r11) : POH_ROTR(e, 11)) ^
+                      (NS1 >= 3 ? rotr_mul(e, M.r25) : POH_ROTR(e, 25));
+        uint32_t S0 = (NS0 >= 1 ? rotr_mul(a, M.r2) : POH_ROTR(a, 2)) ^
+                      (NS0 >= 2 ? rotr_mul(a, M.r13) : POH_ROTR(a, 13)) ^
+                      (NS0 >= 3 ? rotr_mul(a, M.r22) : POH_ROTR(a, 22));
+        uint32_t t1 = h + S1 + ((e & f) ^ (~e & g)) + poh_k(t) + x;
+        uint32_t t2 = S0 + ((a & b) | (c & (a | b)));
         h = g;
         g = f;
         f = e;

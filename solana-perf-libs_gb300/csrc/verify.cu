@@ -28,6 +28,9 @@
 #include "sc25519.cuh"
 
 #define VERIFY_THREADS 128
+#ifndef VERIFY_MIN_BLOCKS
+#define VERIFY_MIN_BLOCKS 1
+#endif
 
 namespace {
 
@@ -201,7 +204,7 @@ __device__ bool verify_one(const SigBatch& a, const uint32_t* sVB, uint32_t i) {
     return diff == 0;
 }
 
-__global__ void __launch_bounds__(VERIFY_THREADS) ed25519_verify_kernel(SigBatch a) {
+__global__ void __launch_bounds__(VERIFY_THREADS, VERIFY_MIN_BLOCKS) ed25519_verify_kernel(SigBatch a) {
     __shared__ uint32_t sVB[VB_WORDS * VB_ENTRIES];
     for (int k = threadIdx.x; k < VB_WORDS * VB_ENTRIES; k += blockDim.x) sVB[k] = a.tables->vb[k];
     __syncthreads();
