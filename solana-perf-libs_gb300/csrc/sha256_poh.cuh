@@ -40,11 +40,22 @@ __device__ __forceinline__ uint32_t rotr_mul(uint32_t x, uint32_t m) {
 
 // Multipliers 2^(32-n) for every SHA-256 rotation, built from a runtime 1.
 struct PohMul {
-    uint32_t r2, r13, r22, r6, r11, r25, r7, r18, r17, r19;
-    __device__ explicit PohMul(uint32_t one)
-        : r2(one << 30), r13(one << 19), r22(one << 10), r6(one << 26), r11(one << 21), r25(one << 7),
+    uint32_t one, r2, r13, r22, r6, r11, r25, r7, r18, r17, r19;
+    __device__ explicit PohMul(uint32_t o)
+        : one(o), r2(o << 30), r13(one << 19), r22(one << 10), r6(one << 26), r11(one << 21), r25(one << 7),
           r7(one << 25), r18(one << 14), r17(one << 15), r19(one << 13) {}
 };
+
+// x + y on the multiply pipe (x * one + y with a runtime one).
+__device__ __forceinline__ uint32_t add_mul(uint32_t x, uint32_t y, uint32_t one) {
+    uint32_t r;
+    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(x), "r"(one), "r"(y));
+    return r;
+}
+
+#ifndef POH_ADD_MUL
+#define POH_ADD_MUL 0
+#endif
 
 // w[0..7]: the 32-byte hash as big-endian words; replaced by SHA-256(w).
 // NS0 / NS1 of the three rotations in Sigma0 / Sigma1 of every round, and NSG
@@ -74,7 +85,10 @@ __device__ __forceinline__ void poh_step_mix(uint32_t w[8], const PohMul& M) {
                           (NSG >= 2 ? rotr_mul(w15, M.r18) : POH_ROTR(w15, 18)) ^ (w15 >> 3);
             uint32_t s1 = (NSG >= 1 ? rotr_mul(w2, M.r17) : POH_ROTR(w2, 17)) ^
                           (NSG >= 2 ? rotr_mul(w2, M.r19) : POH_ROTR(w2, 19)) ^ (w2 >> 10);
-            x = W[t & 15] + s0 + W[(t - 7) & 15] + s1;
+            if (POH_ADD_MUL)
+                x = add_mul(s1, W[t & 15] + s0 + W[(t - 7) & 15], M.one);
+            else
+                x = W[t & 15] + s0 + W[(t - 7) & 15] + s1;
             W[t & 15] = x;
         }
         uint32_t S1 = (NS1 >= 1 ? rotr_mul(e, M.r6) : POH_ROTR(e, 6)) ^
@@ -88,7 +102,7 @@ __device__ __forceinline__ void poh_step_mix(uint32_t w[8], const PohMul& M) {
         h = g;
         g = f;
         f = e;
-        e = d + t1;
+        e = POH_ADD_MUL ? add_mul(d, t1, M.one) : d + t1;
         d = c;
         c = b;
         b = a;

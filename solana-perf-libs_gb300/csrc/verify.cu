@@ -27,7 +27,9 @@
 #include "sha512.cuh"
 #include "sc25519.cuh"
 
+#ifndef VERIFY_THREADS
 #define VERIFY_THREADS 128
+#endif
 #ifndef VERIFY_MIN_BLOCKS
 #define VERIFY_MIN_BLOCKS 1
 #endif
