@@ -22,12 +22,12 @@ struct fe {
 #define FE_INLINE_MUL 0
 #endif
 #if FE_INLINE_MUL
-__device__ __forceinline__ void fe_mul(fe& r, const fe& a, const fe& b) { fe_mul_ptx(r.v, a.v, b.v); }
+__device__ __forceinline__ void fe_mul(fe& r, const fe& a, const fe& b) { fe_mul_wide_ptx(r.v, a.v, b.v); }
 __device__ __forceinline__ void fe_sq(fe& r, const fe& a) { fe_sq_ptx(r.v, a.v); }
 #else
 static __device__ __noinline__ fe fe_mul_call(const fe a, const fe b) {
     fe r;
-    fe_mul_ptx(r.v, a.v, b.v);
+    fe_mul_wide_ptx(r.v, a.v, b.v);
     return r;
 }
 static __device__ __noinline__ fe fe_sq_call(const fe a) {
