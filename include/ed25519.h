@@ -126,6 +126,46 @@ int gb300_ed25519_keypair_device(const uint8_t* seeds, uint8_t* public_keys, uin
 int gb300_ed25519_create_keypairs(const uint8_t* seeds, uint8_t* public_keys, uint8_t* private_keys,
                                   uint32_t num);
 
+/* One job of a ragged batch: a packet buffer with the reference's
+ * per-signature arrays (offsets relative to this job's packets).  kind 0
+ * verifies (key_offsets = signature offsets, out = num verdict bytes),
+ * kind 1 signs (key_offsets = 64-byte private key offsets, out = 64*num
+ * signature bytes). */
+typedef struct {
+    const uint8_t* packets;
+    uint64_t packets_len;
+    const uint32_t* message_lens;
+    const uint32_t* public_key_offsets;
+    const uint32_t* key_offsets;
+    const uint32_t* message_start_offsets;
+    uint32_t num;
+    uint32_t kind;
+    uint8_t* out;
+} gb300_sig_job;
+
+/* Runs every job in ONE persistent launch (verify chunks first, then sign
+ * chunks, pulled from a device queue by a resident grid whose shape the
+ * autotuner picked), replayed from a captured CUDA graph when the batch
+ * shape repeats.  Results are exactly those of ed25519_verify_many /
+ * ed25519_sign_many on each job.  Total packet bytes must stay below 4 GiB.
+ * Returns a cudaError_t. */
+int gb300_ed25519_batch(const gb300_sig_job* jobs, uint32_t num_jobs);
+
+/* Device-pointer form of one mixed batch: nv verify items and ns sign items
+ * over one device packet buffer; `queue_word` is one device uint32 the
+ * launch uses as its queue head.  Enqueued on `stream`. */
+int gb300_ed25519_batch_device(const uint8_t* packets, uint64_t packets_len,
+                               const uint32_t* v_message_lens, const uint32_t* v_public_key_offsets,
+                               const uint32_t* v_signature_offsets, const uint32_t* v_message_start_offsets,
+                               uint32_t nv, uint8_t* v_out,
+                               const uint32_t* s_message_lens, const uint32_t* s_public_key_offsets,
+                               const uint32_t* s_private_key_offsets, const uint32_t* s_message_start_offsets,
+                               uint32_t ns, uint8_t* s_out, uint32_t* queue_word, void* stream);
+
+/* The autotuner's choices for the current GPU as a JSON object (runs the
+ * tuner on first use); returns the length written (truncated to len - 1). */
+int gb300_crypt_tuning(char* buf, size_t len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -34,6 +34,22 @@ void poh_verify_many_set_verbose(bool val);
  * memory, enqueued on `stream` without synchronising; returns a cudaError_t. */
 int gb300_poh_verify_device(uint8_t* hashes, const uint64_t* num_hashes, uint64_t num_elems, void* stream);
 
+/* Ragged batches: same results as poh_verify_many, computed by one
+ * persistent launch that orders entries longest first (by bit length of the
+ * count) and keeps every lane busy by refilling it from a device queue;
+ * replayed from a captured CUDA graph when the batch shape repeats.
+ * Returns 0 or a cudaError_t. */
+int gb300_poh_verify_batch(uint8_t* hashes, const uint64_t* num_hashes_arr, size_t num_elems);
+
+/* Device-memory scratch the device form needs for num_elems entries. */
+size_t gb300_poh_batch_workspace_size(uint64_t num_elems);
+
+/* Device form: hashes (16-byte aligned), counts and workspace (at least
+ * gb300_poh_batch_workspace_size bytes, 16-byte aligned) in GPU memory;
+ * enqueued on `stream`. */
+int gb300_poh_verify_batch_device(uint8_t* hashes, const uint64_t* num_hashes, uint64_t num_elems,
+                                  void* workspace, size_t workspace_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

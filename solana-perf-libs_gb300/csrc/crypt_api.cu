@@ -15,8 +15,10 @@
 //     when the pool is created.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -25,6 +27,8 @@
 #include "poh_verify.h"
 #include "kernels.h"
 #include "tables.cuh"
+
+#include <functional>
 
 namespace {
 
@@ -88,25 +92,54 @@ struct HostBuf {
     }
 };
 
+// A captured launch sequence, replayed while its key (sizes, buffer
+// addresses, launch shape) stays the same.
+struct GraphCache {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<uint64_t> key;
+    void reset() {
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
+        key.clear();
+    }
+};
+
 struct Queue {
     std::mutex mu;
     cudaStream_t stream = nullptr;
-    DevBuf d_data, d_index, d_out;
+    DevBuf d_data, d_index, d_out, d_scratch;
     HostBuf h_stage, h_out;
+    GraphCache g_poh, g_sig;
     void release_buffers() {
+        g_poh.reset();
+        g_sig.reset();
         d_data.release();
         d_index.release();
         d_out.release();
+        d_scratch.release();
         h_stage.release();
         h_out.release();
     }
 };
 
+// Launch shapes picked by the autotuner (tune_device) for one GPU.
+struct Tuning {
+    int sig_threads = 128;        // threads per block of the persistent sign/verify kernel
+    int sig_blocks_per_sm = 0;    // 0 = as many as fit
+    int poh_warps_per_smsp = 1;   // resident warps of the persistent PoH kernel per SM sub-partition
+    double sig_ms[3] = {0, 0, 0}; // calibration times for 64 / 128 / 256 threads
+    double poh_ms[2] = {0, 0};    // calibration times for 1 / 2 warps per sub-partition
+    int calib_sigs = 0, calib_chains = 0;
+};
+
 struct Device {
     int id = -1;
+    int sms = 0;
     CurveTables* tables = nullptr;
     Queue q[kQueues];
     uint32_t next_queue = 0;
+    std::once_flag tuned;
+    Tuning tune;
 };
 
 std::mutex g_mu;
@@ -133,6 +166,7 @@ bool init_locked() {
         for (int k = 0; k < kQueues && ok; k++)
             ok = cudaStreamCreateWithFlags(&D.q[k].stream, cudaStreamNonBlocking) == cudaSuccess;
         if (ok) ok = crypt_tables_create(&D.tables, D.q[0].stream) == cudaSuccess;
+        if (ok) ok = cudaDeviceGetAttribute(&D.sms, cudaDevAttrMultiProcessorCount, d) == cudaSuccess;
         if (!ok) {
             fprintf(stderr, "libcuda-crypt: GPU %d unusable: %s\n", d, cudaGetErrorString(cudaGetLastError()));
             break;
@@ -192,6 +226,193 @@ bool is_page_locked(const void* p) {
         cudaError_t _e = (expr);                    \
         if (_e != cudaSuccess) return _e;           \
     } while (0)
+
+
+template <class F>
+cudaError_t run_graph(GraphCache& gc, const std::vector<uint64_t>& key, cudaStream_t s, F&& enqueue) {
+    if (gc.exec && gc.key == key) return cudaGraphLaunch(gc.exec, s);
+    gc.reset();
+    cudaGraph_t g = nullptr;
+    TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = enqueue(s);
+    cudaError_t e2 = cudaStreamEndCapture(s, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return e != cudaSuccess ? e : e2;
+    }
+    e = cudaGraphInstantiate(&gc.exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        gc.exec = nullptr;
+        return e;
+    }
+    gc.key = key;
+    return cudaGraphLaunch(gc.exec, s);
+}
+
+int env_int(const char* name, int dflt) {
+    const char* v = getenv(name);
+    return v && *v ? atoi(v) : dflt;
+}
+
+uint64_t splitmix(uint64_t& x) {
+    uint64_t z = (x += 0x9e3779b97f4a7c15ull);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+float time_ms(cudaStream_t s, const std::function<cudaError_t()>& f, cudaError_t& err) {
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, s);
+    err = f();
+    cudaEventRecord(b, s);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return ms;
+}
+
+// Calibrates the persistent kernels on this GPU (about a few hundred ms,
+// once per device): the sign/verify kernel on valid signatures it makes with
+// its own keypair and sign kernels, the PoH kernel on ragged chains.
+// GB300_CRYPT_SIG_THREADS / GB300_CRYPT_SIG_BLOCKS /
+// GB300_CRYPT_POH_WARPS_PER_SMSP override the choices.
+void tune_device(Device& D) {
+    Tuning& T = D.tune;
+    cudaStream_t s = nullptr;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return;
+    const int sms = D.sms > 0 ? D.sms : 1;
+    // ---- signatures ----
+    const uint32_t nv = (uint32_t)sms * 128u, ns = nv / 4u, stride = 224u;
+    std::vector<uint8_t> hseed(32ull * nv), hpkt((size_t)stride * nv);
+    std::vector<uint32_t> hidx(4ull * nv + 4ull * ns);
+    uint64_t rs = 0x5eed;
+    for (auto& b : hseed) b = (uint8_t)splitmix(rs);
+    for (size_t i = 0; i < hpkt.size(); i++) hpkt[i] = (uint8_t)splitmix(rs);
+    for (uint32_t i = 0; i < nv; i++) {
+        hidx[i] = 64;                         // v lens
+        hidx[nv + i] = stride * i + 64;       // v pk
+        hidx[2 * nv + i] = stride * i;        // v sig
+        hidx[3 * nv + i] = stride * i + 160;  // v msg
+    }
+    for (uint32_t i = 0; i < ns; i++) {
+        hidx[4 * nv + i] = 64;
+        hidx[4 * nv + ns + i] = stride * i + 64;
+        hidx[4 * nv + 2 * ns + i] = stride * i + 96;   // sk
+        hidx[4 * nv + 3 * ns + i] = stride * i + 160;
+    }
+    uint8_t *dseed = nullptr, *dpk = nullptr, *dsk = nullptr, *dsig = nullptr, *dpkt = nullptr, *dout = nullptr;
+    uint32_t *didx = nullptr, *dq = nullptr;
+    bool ok = cudaMalloc(&dseed, 32ull * nv) == cudaSuccess && cudaMalloc(&dpk, 32ull * nv) == cudaSuccess &&
+              cudaMalloc(&dsk, 64ull * nv) == cudaSuccess && cudaMalloc(&dsig, 64ull * nv) == cudaSuccess &&
+              cudaMalloc(&dpkt, hpkt.size()) == cudaSuccess && cudaMalloc(&dout, nv + 64ull * ns) == cudaSuccess &&
+              cudaMalloc(&didx, 4ull * hidx.size()) == cudaSuccess && cudaMalloc(&dq, 16) == cudaSuccess;
+    if (ok) {
+        cudaMemcpyAsync(dseed, hseed.data(), hseed.size(), cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(dpkt, hpkt.data(), hpkt.size(), cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(didx, hidx.data(), 4ull * hidx.size(), cudaMemcpyHostToDevice, s);
+        launch_ed25519_keypair(dseed, dpk, dsk, nv, D.tables, s);
+        cudaMemcpy2DAsync(dpkt + 64, stride, dpk, 32, 32, nv, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpy2DAsync(dpkt + 96, stride, dsk, 64, 64, nv, cudaMemcpyDeviceToDevice, s);
+        SigBatch sb{dpkt, hpkt.size(), didx, didx + nv, nullptr, didx + 3 * nv, nv, dsig, D.tables};
+        // sign every packet (private key at +96) to get valid signatures
+        std::vector<uint32_t> skoff(nv);
+        for (uint32_t i = 0; i < nv; i++) skoff[i] = stride * i + 96;
+        uint32_t* dsko = nullptr;
+        if (cudaMalloc(&dsko, 4ull * nv) == cudaSuccess) {
+            cudaMemcpyAsync(dsko, skoff.data(), 4ull * nv, cudaMemcpyHostToDevice, s);
+            sb.signature_offsets = dsko;
+            launch_ed25519_sign(sb, s);
+            cudaMemcpy2DAsync(dpkt, stride, dsig, 64, 64, nv, cudaMemcpyDeviceToDevice, s);
+            cudaStreamSynchronize(s);
+            cudaFree(dsko);
+        }
+        SigWork w;
+        w.v = SigBatch{dpkt, hpkt.size(), didx, didx + nv, didx + 2 * nv, didx + 3 * nv, nv, dout, D.tables};
+        w.s = SigBatch{dpkt, hpkt.size(), didx + 4 * nv, didx + 4 * nv + ns, didx + 4 * nv + 2 * ns,
+                       didx + 4 * nv + 3 * ns, ns, dout + nv, D.tables};
+        w.sign_base = (nv + 31u) / 32u * 32u;
+        w.total_chunks = (w.sign_base + ns + 31u) / 32u;
+        w.next = dq;
+        const int cand[3] = {64, 128, 256};
+        double best = 1e30;
+        for (int c = 0; c < 3; c++) {
+            cudaError_t err = cudaSuccess;
+            launch_sig_batch(w, cand[c], 0, sms, s);   // warm
+            cudaStreamSynchronize(s);
+            float ms = 1e30f;
+            for (int r = 0; r < 2; r++) {
+                float t = time_ms(s, [&]() { return launch_sig_batch(w, cand[c], 0, sms, s); }, err);
+                if (err == cudaSuccess && t < ms) ms = t;
+            }
+            T.sig_ms[c] = ms;
+            if (ms < best) {
+                best = ms;
+                T.sig_threads = cand[c];
+            }
+        }
+        T.calib_sigs = (int)(nv + ns);
+    }
+    cudaFree(dseed); cudaFree(dpk); cudaFree(dsk); cudaFree(dsig); cudaFree(dpkt); cudaFree(dout); cudaFree(didx);
+    // ---- PoH ----
+    const uint32_t nc = (uint32_t)sms * 4u * 32u * 2u;
+    std::vector<uint8_t> hh(32ull * nc);
+    std::vector<uint64_t> hc(nc);
+    for (auto& b : hh) b = (uint8_t)splitmix(rs);
+    for (auto& c : hc) c = 1 + splitmix(rs) % 2000u;
+    uint8_t* dh = nullptr;
+    uint64_t* dc = nullptr;
+    void* ws = nullptr;
+    if (cudaMalloc(&dh, hh.size()) == cudaSuccess && cudaMalloc(&dc, 8ull * nc) == cudaSuccess &&
+        cudaMalloc(&ws, poh_batch_workspace_size(nc)) == cudaSuccess) {
+        cudaMemcpyAsync(dh, hh.data(), hh.size(), cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(dc, hc.data(), 8ull * nc, cudaMemcpyHostToDevice, s);
+        double best = 1e30;
+        for (int wps = 1; wps <= 2; wps++) {
+            cudaError_t err = cudaSuccess;
+            float ms = time_ms(s, [&]() { return launch_poh_batch(dh, dc, nc, ws, 4 * sms * wps, s); }, err);
+            T.poh_ms[wps - 1] = ms;
+            if (err == cudaSuccess && ms < best) {
+                best = ms;
+                T.poh_warps_per_smsp = wps;
+            }
+        }
+        T.calib_chains = (int)nc;
+    }
+    cudaFree(dh); cudaFree(dc); cudaFree(ws); cudaFree(dq);
+    cudaGetLastError();
+    cudaStreamDestroy(s);
+    T.sig_threads = env_int("GB300_CRYPT_SIG_THREADS", T.sig_threads);
+    T.sig_blocks_per_sm = env_int("GB300_CRYPT_SIG_BLOCKS", T.sig_blocks_per_sm);
+    T.poh_warps_per_smsp = env_int("GB300_CRYPT_POH_WARPS_PER_SMSP", T.poh_warps_per_smsp);
+    LOG("tuned gpu %d: sig threads %d (ms %.3f %.3f %.3f), poh warps/smsp %d (ms %.3f %.3f)\n", D.id, T.sig_threads,
+        T.sig_ms[0], T.sig_ms[1], T.sig_ms[2], T.poh_warps_per_smsp, T.poh_ms[0], T.poh_ms[1]);
+}
+
+Device* current_device() {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!init_locked() || dev < 0 || dev >= g_num_gpus) return nullptr;
+    return &g_dev[dev];
+}
+
+const Tuning& tuning_for(Device& D) {
+    std::call_once(D.tuned, [&]() {
+        int prev = -1;
+        cudaGetDevice(&prev);
+        cudaSetDevice(D.id);
+        tune_device(D);
+        if (prev >= 0) cudaSetDevice(prev);
+    });
+    return D.tune;
+}
 
 // Stages one signature batch, runs verify or sign on it and copies the
 // results into `out` (n bytes, or 64n bytes for signing).
@@ -524,6 +745,205 @@ int gb300_poh_verify_device(uint8_t* hashes, const uint64_t* num_hashes, uint64_
     if ((reinterpret_cast<uintptr_t>(hashes) & 15u) || (reinterpret_cast<uintptr_t>(num_hashes) & 7u))
         return (int)cudaErrorMisalignedAddress;
     return (int)launch_poh_verify(hashes, num_hashes, num_elems, static_cast<cudaStream_t>(stream));
+}
+
+int gb300_crypt_tuning(char* buf, size_t len) {
+    Device* D = current_device();
+    if (!D || !buf || len == 0) return 0;
+    const Tuning& T = tuning_for(*D);
+    int n = snprintf(buf, len,
+                     "{\"device\": %d, \"sms\": %d, \"sig_threads\": %d, \"sig_blocks_per_sm\": %d, "
+                     "\"sig_calibration_ms\": {\"64\": %.4f, \"128\": %.4f, \"256\": %.4f}, "
+                     "\"sig_calibration_items\": %d, \"poh_warps_per_smsp\": %d, "
+                     "\"poh_calibration_ms\": {\"1\": %.4f, \"2\": %.4f}, \"poh_calibration_chains\": %d}",
+                     D->id, D->sms, T.sig_threads, T.sig_blocks_per_sm, T.sig_ms[0], T.sig_ms[1], T.sig_ms[2],
+                     T.calib_sigs, T.poh_warps_per_smsp, T.poh_ms[0], T.poh_ms[1], T.calib_chains);
+    return n < 0 ? 0 : (n < (int)len ? n : (int)len - 1);
+}
+
+size_t gb300_poh_batch_workspace_size(uint64_t num_elems) { return poh_batch_workspace_size(num_elems); }
+
+int gb300_poh_verify_batch_device(uint8_t* hashes, const uint64_t* num_hashes, uint64_t num_elems, void* workspace,
+                                  size_t workspace_bytes, void* stream) {
+    if (num_elems == 0) return 0;
+    if (num_elems > 0xffffffffull) return (int)cudaErrorInvalidValue;
+    if ((reinterpret_cast<uintptr_t>(hashes) & 15u) || (reinterpret_cast<uintptr_t>(num_hashes) & 7u) ||
+        (reinterpret_cast<uintptr_t>(workspace) & 15u))
+        return (int)cudaErrorMisalignedAddress;
+    if (workspace_bytes < poh_batch_workspace_size(num_elems)) return (int)cudaErrorInvalidValue;
+    Device* D = current_device();
+    if (!D) return (int)cudaErrorNoDevice;
+    const Tuning& T = tuning_for(*D);
+    return (int)launch_poh_batch(hashes, num_hashes, num_elems, workspace, 4 * D->sms * T.poh_warps_per_smsp,
+                                 static_cast<cudaStream_t>(stream));
+}
+
+int gb300_poh_verify_batch(uint8_t* hashes, const uint64_t* num_hashes_arr, size_t num_elems) {
+    if (num_elems == 0) return 0;
+    if (!hashes || !num_hashes_arr || num_elems > 0xffffffffull) return (int)cudaErrorInvalidValue;
+    Lease L;
+    if (!acquire(L)) return 1;
+    const Tuning& T = tuning_for(*L.dev);
+    Queue& Q = *L.q;
+    cudaStream_t s = Q.stream;
+    const size_t hb = 32ull * num_elems, cb = 8ull * num_elems, wb = poh_batch_workspace_size(num_elems);
+    const int warps = 4 * L.dev->sms * T.poh_warps_per_smsp;
+    auto run = [&]() -> cudaError_t {
+        TRY(Q.d_data.ensure(hb + cb));
+        TRY(Q.d_scratch.ensure(wb));
+        TRY(Q.h_stage.ensure(hb + cb));
+        uint8_t* st = static_cast<uint8_t*>(Q.h_stage.p);
+        memcpy(st, hashes, hb);
+        memcpy(st + hb, num_hashes_arr, cb);
+        uint8_t* d = static_cast<uint8_t*>(Q.d_data.p);
+        const uint64_t* dc = reinterpret_cast<const uint64_t*>(d + hb);
+        TRY(cudaMemcpyAsync(d, st, hb + cb, cudaMemcpyHostToDevice, s));
+        std::vector<uint64_t> key = {num_elems, (uint64_t)(uintptr_t)d, (uint64_t)(uintptr_t)Q.d_scratch.p,
+                                     (uint64_t)warps};
+        TRY(run_graph(Q.g_poh, key, s, [&](cudaStream_t cs) {
+            return launch_poh_batch(d, dc, num_elems, Q.d_scratch.p, warps, cs);
+        }));
+        TRY(cudaMemcpyAsync(st, d, hb, cudaMemcpyDeviceToHost, s));
+        TRY(cudaStreamSynchronize(s));
+        memcpy(hashes, st, hb);
+        return cudaSuccess;
+    };
+    cudaError_t e = run();
+    if (e != cudaSuccess) {
+        fprintf(stderr, "libcuda-crypt: gb300_poh_verify_batch failed: %s\n", cudaGetErrorString(e));
+        cudaGetLastError();
+    }
+    return t_last_error = (int)e;
+}
+
+int gb300_ed25519_batch_device(const uint8_t* packets, uint64_t packets_len, const uint32_t* v_message_lens,
+                               const uint32_t* v_public_key_offsets, const uint32_t* v_signature_offsets,
+                               const uint32_t* v_message_start_offsets, uint32_t nv, uint8_t* v_out,
+                               const uint32_t* s_message_lens, const uint32_t* s_public_key_offsets,
+                               const uint32_t* s_private_key_offsets, const uint32_t* s_message_start_offsets,
+                               uint32_t ns, uint8_t* s_out, uint32_t* queue_word, void* stream) {
+    if (nv == 0 && ns == 0) return 0;
+    if ((reinterpret_cast<uintptr_t>(packets) | reinterpret_cast<uintptr_t>(queue_word)) & 3u)
+        return (int)cudaErrorMisalignedAddress;
+    if (ns && (reinterpret_cast<uintptr_t>(s_out) & 3u)) return (int)cudaErrorMisalignedAddress;
+    Device* D = current_device();
+    if (!D) return (int)cudaErrorNoDevice;
+    const Tuning& T = tuning_for(*D);
+    SigWork w;
+    w.v = SigBatch{packets, packets_len, v_message_lens, v_public_key_offsets, v_signature_offsets,
+                   v_message_start_offsets, nv, v_out, D->tables};
+    w.s = SigBatch{packets, packets_len, s_message_lens, s_public_key_offsets, s_private_key_offsets,
+                   s_message_start_offsets, ns, s_out, D->tables};
+    w.sign_base = (nv + 31u) / 32u * 32u;
+    w.total_chunks = (w.sign_base + ns + 31u) / 32u;
+    w.next = queue_word;
+    return (int)launch_sig_batch(w, T.sig_threads, T.sig_blocks_per_sm, D->sms, static_cast<cudaStream_t>(stream));
+}
+
+int gb300_ed25519_batch(const gb300_sig_job* jobs, uint32_t num_jobs) {
+    if (num_jobs == 0) return 0;
+    if (!jobs) return t_last_error = (int)cudaErrorInvalidValue;
+    uint64_t nv = 0, ns = 0, total = 0;
+    bool all_locked = true;
+    for (uint32_t j = 0; j < num_jobs; j++) {
+        const gb300_sig_job& J = jobs[j];
+        if (J.num == 0) continue;
+        if (!J.message_lens || !J.public_key_offsets || !J.key_offsets || !J.message_start_offsets || !J.out ||
+            (J.packets_len && !J.packets) || J.kind > 1)
+            return t_last_error = (int)cudaErrorInvalidValue;
+        (J.kind == 0 ? nv : ns) += J.num;
+        total += J.packets_len;
+        if (J.packets_len && all_locked) all_locked = is_page_locked(J.packets);
+    }
+    if (nv + ns == 0) return 0;
+    if (total >= 0xfffffff0ull || nv + ns > 0x7fffffffull) return t_last_error = (int)cudaErrorInvalidValue;
+    Lease L;
+    if (!acquire(L)) return t_last_error = (int)cudaErrorNoDevice;
+    const Tuning& T = tuning_for(*L.dev);
+    Queue& Q = *L.q;
+    cudaStream_t s = Q.stream;
+    auto run = [&]() -> cudaError_t {
+        const size_t idx_bytes = 16ull * (nv + ns), out_bytes = nv + 64ull * ns;
+        const size_t pk_off = round_up(idx_bytes, 256);
+        TRY(Q.d_data.ensure(total + 16));
+        TRY(Q.d_index.ensure(idx_bytes));
+        TRY(Q.d_out.ensure(out_bytes));
+        TRY(Q.d_scratch.ensure(256));
+        TRY(Q.h_stage.ensure(pk_off + (all_locked ? 0 : total)));
+        TRY(Q.h_out.ensure(out_bytes));
+        uint32_t* hv = static_cast<uint32_t*>(Q.h_stage.p);
+        uint32_t* hs = hv + 4 * nv;
+        uint8_t* img = static_cast<uint8_t*>(Q.h_stage.p) + pk_off;
+        uint8_t* dpk = static_cast<uint8_t*>(Q.d_data.p);
+        uint64_t base = 0, iv = 0, is = 0;
+        for (uint32_t j = 0; j < num_jobs; j++) {
+            const gb300_sig_job& J = jobs[j];
+            if (J.num == 0) continue;
+            uint32_t* h = J.kind == 0 ? hv : hs;
+            const uint64_t cnt = J.kind == 0 ? nv : ns;
+            uint64_t& pos = J.kind == 0 ? iv : is;
+            const uint64_t key_len = 64;
+            for (uint32_t i = 0; i < J.num; i++) {
+                const uint64_t m = J.message_lens[i], po = J.public_key_offsets[i], ko = J.key_offsets[i],
+                               mo = J.message_start_offsets[i];
+                const bool ok = po + 32 <= J.packets_len && ko + key_len <= J.packets_len && mo + m <= J.packets_len;
+                h[pos + i] = ok ? (uint32_t)m : 0xffffffffu;         // an out-of-range item fails on the GPU
+                h[cnt + pos + i] = ok ? (uint32_t)(base + po) : 0u;
+                h[2 * cnt + pos + i] = ok ? (uint32_t)(base + ko) : 0u;
+                h[3 * cnt + pos + i] = ok ? (uint32_t)(base + mo) : 0u;
+            }
+            if (J.packets_len) {
+                if (all_locked)
+                    TRY(cudaMemcpyAsync(dpk + base, J.packets, J.packets_len, cudaMemcpyHostToDevice, s));
+                else
+                    memcpy(img + base, J.packets, J.packets_len);
+            }
+            pos += J.num;
+            base += J.packets_len;
+        }
+        TRY(cudaMemcpyAsync(Q.d_index.p, Q.h_stage.p, idx_bytes, cudaMemcpyHostToDevice, s));
+        if (!all_locked && total) TRY(cudaMemcpyAsync(dpk, img, total, cudaMemcpyHostToDevice, s));
+        const uint32_t* dv = static_cast<const uint32_t*>(Q.d_index.p);
+        const uint32_t* ds = dv + 4 * nv;
+        uint8_t* dout = static_cast<uint8_t*>(Q.d_out.p);
+        SigWork w;
+        w.v = SigBatch{dpk, total, dv, dv + nv, dv + 2 * nv, dv + 3 * nv, (uint32_t)nv, dout, L.dev->tables};
+        w.s = SigBatch{dpk, total, ds, ds + ns, ds + 2 * ns, ds + 3 * ns, (uint32_t)ns, dout + nv, L.dev->tables};
+        w.sign_base = (uint32_t)((nv + 31) / 32 * 32);
+        w.total_chunks = (uint32_t)((w.sign_base + ns + 31) / 32);
+        w.next = static_cast<uint32_t*>(Q.d_scratch.p);
+        std::vector<uint64_t> key = {nv, ns, total, (uint64_t)(uintptr_t)dpk, (uint64_t)(uintptr_t)dv,
+                                     (uint64_t)(uintptr_t)dout, (uint64_t)(uintptr_t)w.next,
+                                     (uint64_t)T.sig_threads, (uint64_t)T.sig_blocks_per_sm};
+        const int sms = L.dev->sms;
+        TRY(run_graph(Q.g_sig, key, s, [&](cudaStream_t cs) {
+            return launch_sig_batch(w, T.sig_threads, T.sig_blocks_per_sm, sms, cs);
+        }));
+        TRY(cudaMemcpyAsync(Q.h_out.p, dout, out_bytes, cudaMemcpyDeviceToHost, s));
+        TRY(cudaStreamSynchronize(s));
+        const uint8_t* ho = static_cast<const uint8_t*>(Q.h_out.p);
+        uint64_t ov = 0, os = 0;
+        for (uint32_t j = 0; j < num_jobs; j++) {
+            const gb300_sig_job& J = jobs[j];
+            if (J.num == 0) continue;
+            if (J.kind == 0) {
+                memcpy(J.out, ho + ov, J.num);
+                ov += J.num;
+            } else {
+                memcpy(J.out, ho + nv + 64 * os, 64ull * J.num);
+                os += J.num;
+            }
+        }
+        return cudaSuccess;
+    };
+    cudaError_t e = run();
+    if (e != cudaSuccess) {
+        fprintf(stderr, "libcuda-crypt: gb300_ed25519_batch failed: %s\n", cudaGetErrorString(e));
+        cudaGetLastError();
+        for (uint32_t j = 0; j < num_jobs; j++)
+            if (jobs[j].out && jobs[j].num) memset(jobs[j].out, 0, jobs[j].kind == 0 ? jobs[j].num : 64ull * jobs[j].num);
+    }
+    return t_last_error = (int)e;
 }
 
 }  // extern "C"

@@ -40,3 +40,22 @@ cudaError_t launch_check_small_order(const uint8_t* points, uint8_t* out, uint32
 
 // PoH: hashes[32*i..] <- SHA-256^num_hashes[i] (hashes[32*i..]), in place.
 cudaError_t launch_poh_verify(uint8_t* hashes, const uint64_t* num_hashes, uint64_t n, cudaStream_t s);
+
+// Ragged PoH batch in one persistent launch (poh_batch.cu): entries ordered
+// longest first, `warps` resident warps refilling lanes from a queue.
+// `workspace` holds poh_batch_workspace_size(n) bytes of device memory.
+size_t poh_batch_workspace_size(uint64_t n);
+cudaError_t launch_poh_batch(uint8_t* hashes, const uint64_t* counts, uint64_t n, void* workspace, int warps,
+                             cudaStream_t s);
+
+// Mixed verify + sign work for one persistent launch (sig_batch.cu).  Both
+// batches index the same packet buffer.  Verify items are chunks
+// [0, ceil(v.n / 32)); sign items start at chunk sign_base / 32.
+struct SigWork {
+    SigBatch v;              // out = v.n verdict bytes
+    SigBatch s;              // out = s.n * 64 signature bytes
+    uint32_t sign_base;      // first sign item's queue position (multiple of 32)
+    uint32_t total_chunks;   // chunks of 32 items
+    uint32_t* next;          // queue head, device word (reset by the launch)
+};
+cudaError_t launch_sig_batch(const SigWork& w, int threads, int blocks_per_sm, int sms, cudaStream_t s);

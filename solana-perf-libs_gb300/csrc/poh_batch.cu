@@ -1,0 +1,132 @@
+// Ragged PoH batches: one persistent launch, longest chain first, lanes
+// refilled from a shared queue.
+//
+// The plain form (poh.cu, the reference's poh_verify_kernel shape) gives each
+// thread one entry for the whole launch: with counts spread over 1..1e6 a
+// warp runs as long as its longest lane and, past 32 * (warps resident)
+// entries, whole waves wait for the slowest warp of the previous wave.
+// Here:
+//   1. order    entries bucketed by bit length of num_hashes, longest
+//               bucket first (three small kernels: histogram, scan, scatter);
+//   2. persist  one warp per SM sub-partition; every lane whose chain is done
+//               stores it and takes the next entry of the order (one
+//               atomicAdd per warp per refill round, ranks by ballot), so the
+//               warp keeps 32 chains in flight until the queue is empty.
+// Results are independent of which lane runs which entry.
+//
+// Scratch (PohBatchScratch) lives in caller-owned device memory:
+// gb300_poh_batch_workspace_size(n) bytes.
+#include <cuda_runtime.h>
+#include "kernels.h"
+#include "sha256_poh.cuh"
+
+namespace {
+
+constexpr int kBuckets = 65;   // bit length of num_hashes: 0..64
+
+struct PohBatchScratch {
+    uint32_t hist[kBuckets];
+    uint32_t cursor[kBuckets];
+    uint32_t next;              // queue head
+    uint32_t pad[3];
+    uint32_t order[1];          // n entries
+};
+
+__device__ __forceinline__ uint32_t bswap_u32(uint32_t x) { return __byte_perm(x, 0, 0x0123); }
+
+__device__ __forceinline__ int bucket_of(uint64_t c) { return c ? 64 - __clzll((long long)c) : 0; }
+
+__global__ void poh_hist_kernel(const uint64_t* counts, uint64_t n, PohBatchScratch* s) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) atomicAdd(&s->hist[bucket_of(counts[i])], 1u);
+}
+
+// single warp: cursor[b] = number of entries in buckets above b (longest first)
+__global__ void poh_scan_kernel(PohBatchScratch* s) {
+    if (threadIdx.x != 0) return;
+    uint32_t run = 0;
+    for (int b = kBuckets - 1; b >= 0; b--) {
+        s->cursor[b] = run;
+        run += s->hist[b];
+    }
+    s->next = 0;
+}
+
+__global__ void poh_scatter_kernel(const uint64_t* counts, uint64_t n, PohBatchScratch* s) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) s->order[atomicAdd(&s->cursor[bucket_of(counts[i])], 1u)] = (uint32_t)i;
+}
+
+__device__ __forceinline__ void load_entry(const uint8_t* hashes, uint32_t e, uint32_t w[8]) {
+    const uint4* p = reinterpret_cast<const uint4*>(hashes + 32ull * e);
+    uint4 lo = p[0], hi = p[1];
+    w[0] = bswap_u32(lo.x); w[1] = bswap_u32(lo.y); w[2] = bswap_u32(lo.z); w[3] = bswap_u32(lo.w);
+    w[4] = bswap_u32(hi.x); w[5] = bswap_u32(hi.y); w[6] = bswap_u32(hi.z); w[7] = bswap_u32(hi.w);
+}
+
+__device__ __forceinline__ void store_entry(uint8_t* hashes, uint32_t e, const uint32_t w[8]) {
+    uint4* p = reinterpret_cast<uint4*>(hashes + 32ull * e);
+    p[0] = make_uint4(bswap_u32(w[0]), bswap_u32(w[1]), bswap_u32(w[2]), bswap_u32(w[3]));
+    p[1] = make_uint4(bswap_u32(w[4]), bswap_u32(w[5]), bswap_u32(w[6]), bswap_u32(w[7]));
+}
+
+__global__ void __launch_bounds__(32) poh_persistent_kernel(uint8_t* hashes, const uint64_t* counts, uint32_t n,
+                                                            PohBatchScratch* s, uint32_t one) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const PohMul M(one);
+    uint32_t w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    uint64_t rem = 0;
+    uint32_t cur = 0xffffffffu;
+    bool done = false;
+    for (;;) {
+        // refill every idle lane (several rounds when entries have count 0)
+        for (;;) {
+            const bool need = !done && rem == 0;
+            const uint32_t mask = __ballot_sync(0xffffffffu, need);
+            if (mask == 0) break;
+            if (need && cur != 0xffffffffu) {
+                store_entry(hashes, cur, w);
+                cur = 0xffffffffu;
+            }
+            uint32_t base = 0;
+            if (lane == (uint32_t)(__ffs(mask) - 1)) base = atomicAdd(&s->next, (uint32_t)__popc(mask));
+            base = __shfl_sync(0xffffffffu, base, __ffs(mask) - 1);
+            if (need) {
+                const uint32_t k = base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+                if (k >= n) {
+                    done = true;
+                } else {
+                    cur = s->order[k];
+                    load_entry(hashes, cur, w);
+                    rem = counts[cur];
+                }
+            }
+        }
+        if (__all_sync(0xffffffffu, done)) break;
+        if (!done) {
+            poh_step_mix<0, 0, 0>(w, M);
+            rem--;
+        }
+    }
+}
+
+}  // namespace
+
+size_t poh_batch_workspace_size(uint64_t n) { return sizeof(PohBatchScratch) + 4ull * (n ? n : 1); }
+
+cudaError_t launch_poh_batch(uint8_t* hashes, const uint64_t* counts, uint64_t n, void* workspace,
+                             int warps, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    if (n > 0xffffffffull) return cudaErrorInvalidValue;
+    PohBatchScratch* sc = static_cast<PohBatchScratch*>(workspace);
+    cudaError_t e = cudaMemsetAsync(sc, 0, sizeof(PohBatchScratch), s);
+    if (e != cudaSuccess) return e;
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    poh_hist_kernel<<<blocks, 256, 0, s>>>(counts, n, sc);
+    poh_scan_kernel<<<1, 32, 0, s>>>(sc);
+    poh_scatter_kernel<<<blocks, 256, 0, s>>>(counts, n, sc);
+    uint64_t need = (n + 31) / 32;
+    unsigned grid = (unsigned)(need < (uint64_t)warps ? need : (uint64_t)warps);
+    poh_persistent_kernel<<<grid, 32, 0, s>>>(hashes, counts, (uint32_t)n, sc, 1u);
+    return cudaGetLastError();
+}

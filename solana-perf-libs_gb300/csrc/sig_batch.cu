@@ -1,0 +1,75 @@
+// Ragged Ed25519 batches: many verify and sign jobs in one persistent launch.
+//
+// The reference's drop-in entry points (and ours, verify.cu / sign.cu) take
+// one batch per call: one launch, one copy each way, one synchronisation, and
+// a grid sized to that batch, so a small batch leaves most SMs idle while
+// the host pays the fixed cost per call.  Here all jobs are concatenated:
+//   * items are split into chunks of 32 (one warp); verify chunks come first
+//     (a verification costs about four signings: longest first), sign chunks
+//     start at the next multiple of 32;
+//   * a persistent grid (blocks resident on every SM, threads per block and
+//     blocks per SM chosen by the autotuner) pulls chunks from a queue head
+//     in device memory until the queue is empty, so a warp that drew cheap
+//     chunks (early rejections, short messages) simply takes more;
+//   * each block stages the verify basepoint table into shared memory once.
+#include <cuda_runtime.h>
+#include "kernels.h"
+#include "tables.cuh"
+#include "sha512.cuh"
+#include "sc25519.cuh"
+
+namespace {
+
+#include "ed25519_ops.cuh"
+
+template <int T>
+__global__ void __launch_bounds__(T) sig_persistent_kernel(SigWork w) {
+    __shared__ uint32_t sVB[VB_WORDS * VB_ENTRIES];
+    for (int k = threadIdx.x; k < VB_WORDS * VB_ENTRIES; k += blockDim.x) sVB[k] = w.v.tables->vb[k];
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31u;
+    for (;;) {
+        uint32_t c = 0;
+        if (lane == 0) c = atomicAdd(w.next, 1u);
+        c = __shfl_sync(0xffffffffu, c, 0);
+        if (c >= w.total_chunks) break;
+        const uint32_t start = c * 32u;
+        if (start < w.sign_base) {
+            const uint32_t i = start + lane;
+            if (i < w.v.n) w.v.out[i] = verify_one(w.v, sVB, i) ? 1 : 0;
+        } else {
+            const uint32_t i = start - w.sign_base + lane;
+            if (i < w.s.n) sign_one(w.s, i);
+        }
+    }
+}
+
+template <int T>
+cudaError_t launch_t(const SigWork& w, int blocks_per_sm, int sms, cudaStream_t s) {
+    int maxb = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, sig_persistent_kernel<T>, T, 0);
+    if (e != cudaSuccess) return e;
+    if (maxb < 1) maxb = 1;
+    int b = blocks_per_sm < 1 ? maxb : (blocks_per_sm < maxb ? blocks_per_sm : maxb);
+    uint32_t warps_needed = w.total_chunks;
+    uint32_t grid = (uint32_t)(b * sms);
+    uint32_t per_block = T / 32;
+    if (grid * per_block > warps_needed) grid = (warps_needed + per_block - 1) / per_block;
+    if (grid == 0) return cudaSuccess;
+    sig_persistent_kernel<T><<<grid, T, 0, s>>>(w);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_sig_batch(const SigWork& w, int threads, int blocks_per_sm, int sms, cudaStream_t s) {
+    if (w.total_chunks == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(w.next, 0, sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    switch (threads) {
+        case 32: return launch_t<32>(w, blocks_per_sm, sms, s);
+        case 64: return launch_t<64>(w, blocks_per_sm, sms, s);
+        case 256: return launch_t<256>(w, blocks_per_sm, sms, s);
+        default: return launch_t<128>(w, blocks_per_sm, sms, s);
+    }
+}

@@ -36,175 +36,7 @@
 
 namespace {
 
-// Carry into each signed radix-16 digit of a scalar < 2^253 (bit i = carry
-// into digit i); digit_i = nibble_i + c_i - 16 c_{i+1}, in [-8, 8].
-__device__ __forceinline__ uint64_t radix16_carries(const uint32_t h[8]) {
-    uint64_t cin = 0;
-    uint32_t c = 0;
-#pragma unroll
-    for (int i = 0; i < 64; i++) {
-        cin |= (uint64_t)c << i;
-        uint32_t v = ((h[i >> 3] >> ((i & 7) * 4)) & 15u) + c;
-        c = v >= 8u;
-    }
-    return cin;
-}
-
-// Same for signed radix-256 digits of S < 2^252, digits in [-128, 128].
-__device__ __forceinline__ uint32_t radix256_carries(const uint32_t s[8]) {
-    uint32_t cin = 0, c = 0;
-#pragma unroll
-    for (int k = 0; k < 32; k++) {
-        cin |= c << k;
-        uint32_t v = ((s[k >> 2] >> ((k & 3) * 8)) & 255u) + c;
-        c = v >= 128u;
-    }
-    return cin;
-}
-
-__device__ __forceinline__ void shl_words(uint32_t w[8], int bits) {
-#pragma unroll
-    for (int i = 7; i > 0; i--) w[i] = __funnelshift_l(w[i - 1], w[i], bits);
-    w[0] <<= bits;
-}
-
-__device__ __forceinline__ void load_vb(ge_niels& n, const uint32_t* sVB, int e) {
-#pragma unroll
-    for (int w = 0; w < 8; w++) {
-        n.YpX.v[w] = sVB[(0 + w) * VB_ENTRIES + e];
-        n.YmX.v[w] = sVB[(8 + w) * VB_ENTRIES + e];
-        n.XY2d.v[w] = sVB[(16 + w) * VB_ENTRIES + e];
-    }
-}
-
-__device__ bool verify_one(const SigBatch& a, const uint32_t* sVB, uint32_t i) {
-    const uint64_t so = a.signature_offsets[i];
-    const uint64_t po = a.public_key_offsets[i];
-    const uint64_t mo = a.message_start_offsets[i];
-    const uint32_t m = a.message_lens[i];
-    if (so + 64 > a.packets_len || po + 32 > a.packets_len || mo + m > a.packets_len) return false;
-
-    uint32_t sig[16], pk[8];
-#pragma unroll
-    for (int k = 0; k < 16; k++) sig[k] = ld_u32_any(a.packets, so + 4 * k, a.packets_len);
-#pragma unroll
-    for (int k = 0; k < 8; k++) pk[k] = ld_u32_any(a.packets, po + 4 * k, a.packets_len);
-
-    if (sig[15] & 0xf0000000u) return false;               // S >= 2^252
-    if (enc_is_order4(sig) || enc_is_order4(pk)) return false;
-
-    // h = SHA-512(R || A || M) mod L
-    uint64_t pre[8];
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        pre[k] = ((uint64_t)bswap32(sig[2 * k]) << 32) | bswap32(sig[2 * k + 1]);
-        pre[4 + k] = ((uint64_t)bswap32(pk[2 * k]) << 32) | bswap32(pk[2 * k + 1]);
-    }
-    uint32_t hd[16], h[8];
-    sha512_prefixed(hd, pre, 8, a.packets, a.packets_len, mo, m);
-    sc_reduce512(h, hd);
-
-    // -A
-    const CurveConsts& K = a.tables->K;
-    fe ax, ay;
-    if (!ge_decode(ax, ay, pk, K)) return false;
-    fe_neg(ax, ax);
-
-    // tab[k] = k * (-A), k = 0..8
-    ge_cached tab[9];
-    {
-        fe d2 = K.d2;
-        ge_p3 P1, P2, P3, P4, t3;
-        ge_done t;
-        P1.X = ax;
-        P1.Y = ay;
-        fe_set(P1.Z, 1);
-        fe_mul(P1.T, ax, ay);
-        ge_cached_identity(tab[0]);
-        ge_p3_to_cached(tab[1], P1, d2);
-        ge_dbl(t, P1.X, P1.Y, P1.Z);
-        ge_to_p3(P2, t);
-        ge_p3_to_cached(tab[2], P2, d2);
-        ge_add_cached(t, P2, tab[1], false);
-        ge_to_p3(P3, t);
-        ge_p3_to_cached(tab[3], P3, d2);
-        ge_dbl(t, P2.X, P2.Y, P2.Z);
-        ge_to_p3(P4, t);
-        ge_p3_to_cached(tab[4], P4, d2);
-        ge_add_cached(t, P4, tab[1], false);
-        ge_to_p3(t3, t);
-        ge_p3_to_cached(tab[5], t3, d2);
-        ge_dbl(t, P3.X, P3.Y, P3.Z);
-        ge_to_p3(t3, t);
-        ge_p3_to_cached(tab[6], t3, d2);
-        ge_add_cached(t, t3, tab[1], false);
-        ge_to_p3(t3, t);
-        ge_p3_to_cached(tab[7], t3, d2);
-        ge_dbl(t, P4.X, P4.Y, P4.Z);
-        ge_to_p3(t3, t);
-        ge_p3_to_cached(tab[8], t3, d2);
-    }
-
-    uint32_t hh[8], ss[8];
-#pragma unroll
-    for (int k = 0; k < 8; k++) {
-        hh[k] = h[k];
-        ss[k] = sig[8 + k];
-    }
-    const uint64_t hc = radix16_carries(h);
-    const uint32_t scar = radix256_carries(ss);
-
-    ge_p3 R;
-    ge_p3_identity(R);
-#pragma unroll 1
-    for (int i = 63; i >= 0; i--) {
-        ge_done t;
-        if (i != 63) {
-            ge_p2 q;
-            ge_dbl(t, R.X, R.Y, R.Z);
-            ge_to_p2(q, t);
-            ge_dbl(t, q.X, q.Y, q.Z);
-            ge_to_p2(q, t);
-            ge_dbl(t, q.X, q.Y, q.Z);
-            ge_to_p2(q, t);
-            ge_dbl(t, q.X, q.Y, q.Z);
-            ge_to_p3(R, t);
-        }
-        // digit i of h
-        int nib = (int)(hh[7] >> 28);
-        shl_words(hh, 4);
-        int ci = (int)((hc >> i) & 1u);
-        int cn = (i < 63) ? (int)((hc >> (i + 1)) & 1u) : 0;
-        int da = nib + ci - 16 * cn;
-        int ua = min(da < 0 ? -da : da, 8);      // |digit| <= 8 for h < L; clamp keeps the lookup in the table
-        ge_add_cached(t, R, tab[ua], da < 0);
-        if ((i & 1) == 0) {
-            ge_to_p3(R, t);
-            int k = i >> 1;
-            int byte = (int)(ss[7] >> 24);
-            shl_words(ss, 8);
-            int bc = (int)((scar >> k) & 1u);
-            int bn = (k < 31) ? (int)((scar >> (k + 1)) & 1u) : 0;
-            int db = byte + bc - 256 * bn;
-            int ub = min(db < 0 ? -db : db, VB_ENTRIES - 1);
-            ge_niels nb;
-            load_vb(nb, sVB, ub);
-            ge_add_niels(t, R, nb, db < 0);
-        }
-        ge_p2 q;
-        ge_to_p2(q, t);
-        R.X = q.X;
-        R.Y = q.Y;
-        R.Z = q.Z;
-    }
-
-    uint32_t enc[8];
-    ge_encode_p2(enc, R.X, R.Y, R.Z);
-    uint32_t diff = 0;
-#pragma unroll
-    for (int k = 0; k < 8; k++) diff |= enc[k] ^ sig[k];
-    return diff == 0;
-}
+#include "ed25519_ops.cuh"
 
 __global__ void __launch_bounds__(VERIFY_THREADS, VERIFY_MIN_BLOCKS) ed25519_verify_kernel(SigBatch a) {
     __shared__ uint32_t sVB[VB_WORDS * VB_ENTRIES];

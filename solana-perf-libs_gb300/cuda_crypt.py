@@ -29,6 +29,16 @@ class GpuElems(ctypes.Structure):
     _fields_ = [("elems", _u8p), ("num", ctypes.c_uint32)]
 
 
+class SigJob(ctypes.Structure):
+    """gb300_sig_job: one verify (kind 0) or sign (kind 1) job of a ragged batch."""
+    _fields_ = [("packets", _u8p), ("packets_len", ctypes.c_uint64), ("message_lens", _u32p),
+                ("public_key_offsets", _u32p), ("key_offsets", _u32p), ("message_start_offsets", _u32p),
+                ("num", ctypes.c_uint32), ("kind", ctypes.c_uint32), ("out", _u8p)]
+
+
+JOB_VERIFY, JOB_SIGN = 0, 1
+
+
 def build(jobs: int = 8) -> str:
     """Compile libcuda-crypt.so for sm_103a in place (make, parallel TUs)."""
     subprocess.run(["make", "-s", "-C", HERE, f"-j{jobs}", "libcuda-crypt.so"], check=True)
@@ -102,6 +112,16 @@ class CudaCrypt:
         L.gb300_ed25519_keypair_device.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_uint32, ctypes.c_void_p]
         L.gb300_poh_verify_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p]
         L.gb300_ed25519_create_keypairs.argtypes = [_u8p, _u8p, _u8p, ctypes.c_uint32]
+        L.gb300_ed25519_batch.argtypes = [ctypes.POINTER(SigJob), ctypes.c_uint32]
+        L.gb300_ed25519_batch_device.argtypes = [ctypes.c_void_p, ctypes.c_uint64] + [ctypes.c_void_p] * 4 + \
+            [ctypes.c_uint32, ctypes.c_void_p] + [ctypes.c_void_p] * 4 + [ctypes.c_uint32, ctypes.c_void_p,
+                                                                        ctypes.c_void_p, ctypes.c_void_p]
+        L.gb300_poh_verify_batch.argtypes = [_u8p, _u64p, ctypes.c_size_t]
+        L.gb300_poh_batch_workspace_size.argtypes = [ctypes.c_uint64]
+        L.gb300_poh_batch_workspace_size.restype = ctypes.c_size_t
+        L.gb300_poh_verify_batch_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                                                    ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+        L.gb300_crypt_tuning.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
 
     # ---- reference entry points ------------------------------------------
     def init(self) -> bool:
@@ -183,6 +203,65 @@ class CudaCrypt:
 
     def host_unregister(self, arr: np.ndarray) -> int:
         return int(self.lib.cuda_host_unregister(arr.ctypes.data))
+
+    # ---- ragged batches in one persistent launch -----------------------------
+    def ed25519_batch(self, jobs) -> list:
+        """jobs: list of (SigPackets, kind).  Returns one output array per job
+        (verdicts for kind 0, (n, 64) signatures for kind 1)."""
+        keep, outs = [], []
+        arr = (SigJob * max(1, len(jobs)))()
+        for k, (sp, kind) in enumerate(jobs):
+            pk = np.ascontiguousarray(sp.concatenated(), dtype=np.uint8)
+            arrs = [np.ascontiguousarray(a, dtype=np.uint32) for a in
+                    (sp.message_lens, sp.public_key_offsets, sp.signature_offsets, sp.message_start_offsets)]
+            n = len(arrs[0])
+            out = np.zeros(n if kind == JOB_VERIFY else (n, 64), dtype=np.uint8)
+            keep += [pk] + arrs
+            outs.append(out)
+            j = arr[k]
+            j.packets = _p(pk, _u8p)
+            j.packets_len = pk.nbytes
+            j.message_lens, j.public_key_offsets, j.key_offsets, j.message_start_offsets = \
+                [_p(a, _u32p) for a in arrs]
+            j.num, j.kind, j.out = n, kind, _p(out, _u8p)
+        rc = self.lib.gb300_ed25519_batch(arr, len(jobs))
+        if rc != 0:
+            raise RuntimeError(f"gb300_ed25519_batch: cudaError {rc}")
+        return outs
+
+    def poh_verify_batch(self, hashes: np.ndarray, num_hashes) -> int:
+        """In place on `hashes` (uint8, n*32), like poh_verify_many."""
+        assert hashes.dtype == np.uint8 and hashes.flags["C_CONTIGUOUS"]
+        nh = np.ascontiguousarray(num_hashes, dtype=np.uint64)
+        return int(self.lib.gb300_poh_verify_batch(_p(hashes, _u8p), _p(nh, _u64p), len(nh)))
+
+    def poh_batch_workspace_size(self, n: int) -> int:
+        return int(self.lib.gb300_poh_batch_workspace_size(n))
+
+    def poh_verify_batch_device(self, hashes, num_hashes, workspace, stream=0) -> None:
+        rc = self.lib.gb300_poh_verify_batch_device(hashes.data_ptr(), num_hashes.data_ptr(), num_hashes.numel(),
+                                                    workspace.data_ptr(), workspace.numel() * workspace.element_size(),
+                                                    stream)
+        if rc != 0:
+            raise RuntimeError(f"gb300_poh_verify_batch_device: cudaError {rc}")
+
+    def ed25519_batch_device(self, packets, v, v_out, s, s_out, queue_word, stream=0) -> None:
+        """v / s: 4 device int32 tensors (lens, pubkey, sig-or-privkey, message offsets)."""
+        nv = v[0].numel() if v else 0
+        ns = s[0].numel() if s else 0
+        vp = [t.data_ptr() for t in v] if v else [0, 0, 0, 0]
+        spp = [t.data_ptr() for t in s] if s else [0, 0, 0, 0]
+        rc = self.lib.gb300_ed25519_batch_device(packets.data_ptr(), packets.numel(), *vp, nv,
+                                                 v_out.data_ptr() if nv else 0, *spp, ns,
+                                                 s_out.data_ptr() if ns else 0, queue_word.data_ptr(), stream)
+        if rc != 0:
+            raise RuntimeError(f"gb300_ed25519_batch_device: cudaError {rc}")
+
+    def tuning(self) -> dict:
+        import json
+        buf = ctypes.create_string_buffer(1024)
+        n = self.lib.gb300_crypt_tuning(buf, 1024)
+        return json.loads(buf.value[:n].decode()) if n else {}
 
     # ---- device-pointer forms (torch tensors on the GPU) -------------------
     def verify_device(self, packets, message_lens, public_key_offsets, signature_offsets, message_start_offsets,

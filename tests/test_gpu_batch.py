@@ -1,0 +1,125 @@
+"""Ragged batches in one persistent launch (gb300_ed25519_batch,
+gb300_poh_verify_batch and their device forms): identical results to the
+per-call entry points and to the CPU oracle, including repeated calls that
+replay a captured CUDA graph and calls that change the batch shape."""
+import numpy as np
+import pytest
+
+import workloads
+from cuda_crypt import JOB_SIGN, JOB_VERIFY
+from conftest import nthreads
+
+pytestmark = pytest.mark.gpu
+
+
+def test_poh_batch_ragged(lib, oracle):
+    h, cnt = workloads.poh_ragged(n=3000, max_hashes=20000, seed=61)
+    cnt[:7] = [0, 1, 2, 0, 20000, 31, 32]
+    exp = oracle.poh_verify_many(h, cnt, nthreads())
+    for rep in range(3):                      # first call captures, later calls replay the graph
+        buf = np.ascontiguousarray(h.ravel())
+        assert lib.poh_verify_batch(buf, cnt) == 0
+        assert np.array_equal(buf.reshape(-1, 32), exp), rep
+    # another shape
+    buf = np.ascontiguousarray(h[:1234].ravel())
+    assert lib.poh_verify_batch(buf, cnt[:1234]) == 0
+    assert np.array_equal(buf.reshape(-1, 32), exp[:1234])
+
+
+def test_poh_batch_matches_plain_on_many_chains(lib):
+    """More chains than resident lanes (lanes take several chains each)."""
+    rng = np.random.default_rng(62)
+    n = 40000
+    h = rng.integers(0, 256, (n, 32), dtype=np.uint8)
+    cnt = rng.integers(0, 300, n).astype(np.uint64)
+    a = np.ascontiguousarray(h.ravel())
+    b = a.copy()
+    assert lib.poh_verify_many(a, cnt) == 0
+    assert lib.poh_verify_batch(b, cnt) == 0
+    assert np.array_equal(a, b)
+
+
+def test_poh_batch_device(lib, oracle):
+    torch = pytest.importorskip("torch")
+    h, cnt = workloads.poh_ragged(n=2000, max_hashes=5000, seed=63)
+    exp = oracle.poh_verify_many(h, cnt, nthreads())
+    dh = torch.from_numpy(h.copy()).cuda()
+    dc = torch.from_numpy(cnt.astype(np.int64)).cuda()
+    ws = torch.empty(lib.poh_batch_workspace_size(len(cnt)), dtype=torch.uint8, device="cuda")
+    lib.poh_verify_batch_device(dh, dc, ws, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(dh.cpu().numpy(), exp)
+
+
+def _ragged(oracle, seed, n_batches=5, cap=300):
+    return workloads.ragged_sigs(oracle.create_keypairs, oracle.sign_packets, n_batches=n_batches,
+                                 total_packet_cap=cap, seed=seed)
+
+
+def test_sig_batch_mixed_jobs(lib, oracle):
+    rs = _ragged(oracle, 64)
+    jobs = [(sp, JOB_VERIFY) for sp in rs.verify] + [(sp, JOB_SIGN) for sp in rs.sign]
+    exp = [oracle.verify_packets(sp, nthreads()) for sp in rs.verify] + \
+          [oracle.sign_packets(sp, nthreads()) for sp in rs.sign]
+    for rep in range(3):                      # graph capture, then replays
+        outs = lib.ed25519_batch(jobs)
+        for k, (o, e) in enumerate(zip(outs, exp)):
+            assert np.array_equal(o, e), (rep, k)
+    # interleaved kinds and a different shape
+    jobs2 = [jobs[-1], jobs[0], jobs[-2], jobs[1]]
+    outs = lib.ed25519_batch(jobs2)
+    for o, k in zip(outs, [len(exp) - 1, 0, len(exp) - 2, 1]):
+        assert np.array_equal(o, exp[k])
+
+
+def test_sig_batch_matches_per_call(lib, oracle):
+    rs = _ragged(oracle, 65, n_batches=4, cap=200)
+    outs = lib.ed25519_batch([(sp, JOB_VERIFY) for sp in rs.verify])
+    for o, sp in zip(outs, rs.verify):
+        assert np.array_equal(o, lib.verify_many(sp))
+
+
+def test_sig_batch_out_of_range_items(lib, oracle):
+    sp, _ = workloads.verify_uniform(lib.create_keypairs, lib.sign_many, n=64, seed=66)
+    bad = type(sp)(sp.batches, sp.message_size, sp.message_lens.copy(), sp.public_key_offsets.copy(),
+                   sp.signature_offsets.copy(), sp.message_start_offsets.copy())
+    total = sum(len(b) for b in sp.batches)
+    bad.signature_offsets[3] = total - 8
+    bad.message_lens[5] = 10 ** 9
+    good = lib.verify_many(sp)
+    # another job follows: an out-of-range offset must not read into it
+    outs = lib.ed25519_batch([(bad, JOB_VERIFY), (sp, JOB_VERIFY)])
+    exp = good.copy()
+    exp[3] = 0
+    exp[5] = 0
+    assert np.array_equal(outs[0], exp)
+    assert np.array_equal(outs[1], good)
+
+
+def test_sig_batch_device(lib, oracle):
+    torch = pytest.importorskip("torch")
+    rs = _ragged(oracle, 67, n_batches=1, cap=400)
+    sp, ss = rs.verify[0], rs.sign[0]
+    # put both into one device buffer: verify packets then sign packets
+    pv, ps = sp.concatenated(), ss.concatenated()
+    packets = np.concatenate([pv, ps])
+    off = np.uint32(len(pv))
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    v = [dev(a.astype(np.int32)) for a in (sp.message_lens, sp.public_key_offsets, sp.signature_offsets,
+                                           sp.message_start_offsets)]
+    s = [dev(a.astype(np.int32)) for a in (ss.message_lens, ss.public_key_offsets + off, ss.signature_offsets + off,
+                                           ss.message_start_offsets + off)]
+    v_out = torch.zeros(sp.total_signatures, dtype=torch.uint8, device="cuda")
+    s_out = torch.zeros((ss.total_signatures, 64), dtype=torch.uint8, device="cuda")
+    q = torch.zeros(4, dtype=torch.int32, device="cuda")
+    lib.ed25519_batch_device(dev(packets), v, v_out, s, s_out, q, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(v_out.cpu().numpy(), oracle.verify_packets(sp, nthreads()))
+    assert np.array_equal(s_out.cpu().numpy(), oracle.sign_packets(ss, nthreads()))
+
+
+def test_tuning_report(lib):
+    t = lib.tuning()
+    assert t["sig_threads"] in (64, 128, 256)
+    assert t["poh_warps_per_smsp"] in (1, 2)
+    assert t["sms"] > 0
