@@ -311,7 +311,7 @@ void tune_device(Device& D) {
     uint32_t *didx = nullptr, *dq = nullptr;
     bool ok = cudaMalloc(&dseed, 32ull * nv) == cudaSuccess && cudaMalloc(&dpk, 32ull * nv) == cudaSuccess &&
               cudaMalloc(&dsk, 64ull * nv) == cudaSuccess && cudaMalloc(&dsig, 64ull * nv) == cudaSuccess &&
-              cudaMalloc(&dpkt, hpkt.size()) == cudaSuccess && cudaMalloc(&dout, nv + 64ull * ns) == cudaSuccess &&
+              cudaMalloc(&dpkt, hpkt.size()) == cudaSuccess && cudaMalloc(&dout, round_up(nv, 64) + 64ull * ns) == cudaSuccess &&
               cudaMalloc(&didx, 4ull * hidx.size()) == cudaSuccess && cudaMalloc(&dq, 16) == cudaSuccess;
     if (ok) {
         cudaMemcpyAsync(dseed, hseed.data(), hseed.size(), cudaMemcpyHostToDevice, s);
@@ -336,7 +336,7 @@ void tune_device(Device& D) {
         SigWork w;
         w.v = SigBatch{dpkt, hpkt.size(), didx, didx + nv, didx + 2 * nv, didx + 3 * nv, nv, dout, D.tables};
         w.s = SigBatch{dpkt, hpkt.size(), didx + 4 * nv, didx + 4 * nv + ns, didx + 4 * nv + 2 * ns,
-                       didx + 4 * nv + 3 * ns, ns, dout + nv, D.tables};
+                       didx + 4 * nv + 3 * ns, ns, dout + round_up(nv, 64), D.tables};
         w.sign_base = (nv + 31u) / 32u * 32u;
         w.total_chunks = (w.sign_base + ns + 31u) / 32u;
         w.next = dq;
@@ -863,7 +863,9 @@ int gb300_ed25519_batch(const gb300_sig_job* jobs, uint32_t num_jobs) {
     Queue& Q = *L.q;
     cudaStream_t s = Q.stream;
     auto run = [&]() -> cudaError_t {
-        const size_t idx_bytes = 16ull * (nv + ns), out_bytes = nv + 64ull * ns;
+        // verdicts, then signatures from a 64-byte boundary (32-bit stores)
+        const size_t sig_out_off = round_up(nv, 64);
+        const size_t idx_bytes = 16ull * (nv + ns), out_bytes = sig_out_off + 64ull * ns;
         const size_t pk_off = round_up(idx_bytes, 256);
         TRY(Q.d_data.ensure(total + 16));
         TRY(Q.d_index.ensure(idx_bytes));
@@ -908,7 +910,8 @@ int gb300_ed25519_batch(const gb300_sig_job* jobs, uint32_t num_jobs) {
         uint8_t* dout = static_cast<uint8_t*>(Q.d_out.p);
         SigWork w;
         w.v = SigBatch{dpk, total, dv, dv + nv, dv + 2 * nv, dv + 3 * nv, (uint32_t)nv, dout, L.dev->tables};
-        w.s = SigBatch{dpk, total, ds, ds + ns, ds + 2 * ns, ds + 3 * ns, (uint32_t)ns, dout + nv, L.dev->tables};
+        w.s = SigBatch{dpk, total, ds, ds + ns, ds + 2 * ns, ds + 3 * ns, (uint32_t)ns, dout + sig_out_off,
+                       L.dev->tables};
         w.sign_base = (uint32_t)((nv + 31) / 32 * 32);
         w.total_chunks = (uint32_t)((w.sign_base + ns + 31) / 32);
         w.next = static_cast<uint32_t*>(Q.d_scratch.p);
@@ -930,7 +933,7 @@ int gb300_ed25519_batch(const gb300_sig_job* jobs, uint32_t num_jobs) {
                 memcpy(J.out, ho + ov, J.num);
                 ov += J.num;
             } else {
-                memcpy(J.out, ho + nv + 64 * os, 64ull * J.num);
+                memcpy(J.out, ho + sig_out_off + 64 * os, 64ull * J.num);
                 os += J.num;
             }
         }
