@@ -228,8 +228,11 @@ bool is_page_locked(const void* p) {
     } while (0)
 
 
+// GB300_CRYPT_NO_GRAPH=1 enqueues the launches directly instead.
 template <class F>
 cudaError_t run_graph(GraphCache& gc, const std::vector<uint64_t>& key, cudaStream_t s, F&& enqueue) {
+    static const bool no_graph = getenv("GB300_CRYPT_NO_GRAPH") && atoi(getenv("GB300_CRYPT_NO_GRAPH")) != 0;
+    if (no_graph) return enqueue(s);
     if (gc.exec && gc.key == key) return cudaGraphLaunch(gc.exec, s);
     gc.reset();
     cudaGraph_t g = nullptr;
