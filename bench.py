@@ -268,6 +268,124 @@ def bench_verify_e2e(lib, sp, steps, warmup):
     return s, out
 
 
+def bench_poh_ragged(lib, torch, steps):
+    """16384 entries, num_hashes log-uniform in 1..1e6: plain one-thread-per-
+    entry launch vs the persistent longest-first batch launch."""
+    import workloads
+    h0, cnt = workloads.poh_ragged(16384, 1_000_000, seed=4)
+    stream = torch.cuda.current_stream()
+    d_h0 = torch.from_numpy(h0.copy()).cuda()
+    d_c = torch.from_numpy(cnt.astype(np.int64)).cuda()
+    ws = torch.empty(lib.poh_batch_workspace_size(len(cnt)), dtype=torch.uint8, device="cuda")
+    total = float(cnt.sum())
+    res = {}
+    outs = {}
+    for name in ("plain", "batch"):
+        times = []
+        for it in range(steps + 1):
+            d_h = d_h0.clone()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            if name == "plain":
+                lib.poh_verify_device(d_h, d_c, stream.cuda_stream)
+            else:
+                lib.poh_verify_batch_device(d_h, d_c, ws, stream.cuda_stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if it:
+                times.append(e0.elapsed_time(e1) * 1e-3)
+        outs[name] = d_h.cpu().numpy()
+        res[name] = {"hashes_per_s": total / min(times), "s_per_launch": min(times)}
+    assert np.array_equal(outs["plain"], outs["batch"])
+    hb = h0.ravel().copy()
+    t = time.perf_counter()
+    rc = lib.poh_verify_batch(hb, cnt)
+    e2e = time.perf_counter() - t
+    assert rc == 0 and np.array_equal(hb.reshape(-1, 32), outs["batch"])
+    longest = int(cnt.max())
+    return {"config": {"workload": "16384 entries, num_hashes log-uniform in 1..1e6 (seeded)", "entries": 16384,
+                       "total_hashes": int(total), "longest_chain": longest},
+            "plain_per_call": res["plain"], "batched_persistent": res["batch"],
+            "e2e": {"value": total / e2e, "unit": "hashes/s", "path": "gb300_poh_verify_batch (host buffers)",
+                    "h2d_bytes_per_step": 16384 * 40, "d2h_bytes_per_step": 16384 * 32},
+            "longest_chain_s_at_1332_alu_instr_per_hash": longest * 2 * 1332 / 2.07e9,
+            "note": "makespan is bounded below by the longest chain: a serial SHA-256 chain on one lane, "
+                    "issued at the ALU pipe rate of one warp (2 cycles per warp instruction)"}
+
+
+def bench_ragged_sigs(lib, torch):
+    """64 ragged verify batches (1..8192 packets, 0..1232-byte messages,
+    1..4 signatures per packet, 5% each adversarial class) plus their
+    signing in 128-packet jobs: per-call entry points vs one batch launch."""
+    import workloads
+    from cuda_crypt import JOB_SIGN, JOB_VERIFY
+    t0 = time.perf_counter()
+    rs = workloads.ragged_sigs(lib.create_keypairs, lib.sign_many, seed=3)
+    gen_s = time.perf_counter() - t0
+    nv = sum(sp.total_signatures for sp in rs.verify)
+    ns = sum(sp.total_signatures for sp in rs.sign)
+    jobs = [(sp, JOB_VERIFY) for sp in rs.verify] + [(sp, JOB_SIGN) for sp in rs.sign]
+    # warm both paths
+    lib.ed25519_batch(jobs[:2])
+    lib.verify_many(rs.verify[0])
+    # per-call (the reference's call pattern): one ed25519_verify_many / ed25519_sign_many per job
+    t = time.perf_counter()
+    per_call = [lib.verify_many(sp) for sp in rs.verify] + [lib.sign_many(sp) for sp in rs.sign]
+    t_call = time.perf_counter() - t
+    t = time.perf_counter()
+    batched = lib.ed25519_batch(jobs)
+    t_batch1 = time.perf_counter() - t
+    t = time.perf_counter()
+    batched = lib.ed25519_batch(jobs)        # same shape again: graph replay
+    t_batch = time.perf_counter() - t
+    assert all(np.array_equal(a, b) for a, b in zip(per_call, batched))
+    cls = np.concatenate(rs.classes)
+    ver = np.concatenate(batched[:len(rs.verify)])
+    valid_ok = bool(np.all(ver[cls == workloads.CLASS_VALID] == 1))
+    # device-resident: one persistent launch over everything
+    stream = torch.cuda.current_stream()
+    pk_parts, v_idx, s_idx, base = [], [[], [], [], []], [[], [], [], []], 0
+    for sp in rs.verify:
+        c = sp.concatenated()
+        pk_parts.append(c)
+        for k, a in enumerate((sp.message_lens, sp.public_key_offsets + base, sp.signature_offsets + base,
+                               sp.message_start_offsets + base)):
+            v_idx[k].append(np.asarray(a, dtype=np.int64))
+        base += len(c)
+    for sp in rs.sign:
+        c = sp.concatenated()
+        pk_parts.append(c)
+        for k, a in enumerate((sp.message_lens, sp.public_key_offsets + base, sp.signature_offsets + base,
+                               sp.message_start_offsets + base)):
+            s_idx[k].append(np.asarray(a, dtype=np.int64))
+        base += len(c)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    packets = dev(np.concatenate(pk_parts))
+    v = [dev(np.concatenate(x).astype(np.int32)) for x in v_idx]
+    s_ = [dev(np.concatenate(x).astype(np.int32)) for x in s_idx]
+    v_out = torch.zeros(nv, dtype=torch.uint8, device="cuda")
+    s_out = torch.zeros((ns, 64), dtype=torch.uint8, device="cuda")
+    q = torch.zeros(4, dtype=torch.int32, device="cuda")
+    best = 1e30
+    for it in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        lib.ed25519_batch_device(packets, v, v_out, s_, s_out, q, stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if it:
+            best = min(best, e0.elapsed_time(e1) * 1e-3)
+    assert np.array_equal(v_out.cpu().numpy(), ver)
+    return {"config": {"workload": "64 ragged verify batches + 128-packet sign jobs (seeded; 5% each of S>=L, "
+                                   "small-order A, small-order R, undecodable A, flipped message)",
+                       "verify_signatures": nv, "sign_signatures": ns, "jobs": len(jobs),
+                       "packet_bytes": int(base), "generation_s": gen_s},
+            "per_call_e2e_s": t_call, "batched_e2e_s": t_batch, "batched_first_call_s": t_batch1,
+            "per_call_items_per_s": (nv + ns) / t_call, "batched_items_per_s": (nv + ns) / t_batch,
+            "device_resident_one_launch_s": best, "device_items_per_s": (nv + ns) / best,
+            "results_identical_per_call_vs_batched": True, "valid_class_all_accepted": valid_ok}
+
+
 def cpu_poh(h0, cnt, nthreads, sample_entries):
     from oracle.oracle import get_oracle
     o = get_oracle()
@@ -372,6 +490,10 @@ def run_ours(args):
                                   "cores": nthreads, "kind": "port",
                                   "sample": f"{reps} x 1024 verifies on {nthreads} threads, CPU oracle"}
     line["ed25519_verify"] = verify
+    if not args.skip_ragged:
+        line["poh_ragged"] = bench_poh_ragged(lib, torch, steps=2)
+        line["ragged_sigs"] = bench_ragged_sigs(lib, torch)
+    line["autotuner"] = lib.tuning()
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -464,6 +586,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--case", default=None, help="run one small kernel case (for profiling) and exit")
+    ap.add_argument("--skip-ragged", action="store_true", help="skip the ragged PoH / signature batch sections")
     args = ap.parse_args()
     if args.case:
         run_case(args.case)
