@@ -12,6 +12,9 @@
 //               stores it and takes the next entry of the order (one
 //               atomicAdd per warp per refill round, ranks by ballot), so the
 //               warp keeps 32 chains in flight until the queue is empty.
+//               Between refills all busy lanes step together for the
+//               smallest remaining count among them, so the hashing loop
+//               carries no per-step queue bookkeeping.
 // Results are independent of which lane runs which entry.
 //
 // Scratch (PohBatchScratch) lives in caller-owned device memory:
@@ -103,9 +106,18 @@ __global__ void __launch_bounds__(32) poh_persistent_kernel(uint8_t* hashes, con
             }
         }
         if (__all_sync(0xffffffffu, done)) break;
+        // run every busy lane until the first of them finishes: the inner
+        // loop is then the plain chain loop, with no per-step bookkeeping
+        uint64_t r = done ? ~0ull : rem;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const uint64_t other = __shfl_xor_sync(0xffffffffu, r, o);
+            r = other < r ? other : r;
+        }
         if (!done) {
-            poh_step_mix<0, 0, 0>(w, M);
-            rem--;
+#pragma unroll 1
+            for (uint64_t k = 0; k < r; k++) poh_step_mix<0, 0, 0>(w, M);
+            rem -= r;
         }
     }
 }
