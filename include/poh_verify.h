@@ -50,6 +50,20 @@ size_t gb300_poh_batch_workspace_size(uint64_t num_elems);
 int gb300_poh_verify_batch_device(uint8_t* hashes, const uint64_t* num_hashes, uint64_t num_elems,
                                   void* workspace, size_t workspace_bytes, void* stream);
 
+/* Same work as gb300_poh_verify_batch_device without a workspace argument
+ * and without allocating anything.  No counterpart in the reference.  It is
+ * for callers that may not call cudaMalloc (GPU memory owned by a pooling
+ * allocator with a fixed budget, or a pipeline that must not take the
+ * device-wide synchronisation cudaMalloc/cudaFree can cause): its scratch is
+ * a 1 MiB array built into the library, so at most 262,144 entries per call
+ * (more returns cudaErrorInvalidValue with a message on stderr).  The first
+ * call on each device looks up that array's device address; make that first
+ * call before any stream capture.  All calls share the one array, so calls
+ * that overlap on the GPU (concurrent streams or threads) race: serialise
+ * them.  hashes 16-byte and counts 8-byte aligned; enqueued on `stream`;
+ * returns 0 or a cudaError_t. */
+int gb300_poh_verify_batch_static(uint8_t* hashes, const uint64_t* num_hashes, uint64_t num_elems, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

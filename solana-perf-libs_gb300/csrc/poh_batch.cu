@@ -142,3 +142,71 @@ cudaError_t launch_poh_batch(uint8_t* hashes, const uint64_t* counts, uint64_t n
     poh_persistent_kernel<<<grid, 32, 0, s>>>(hashes, counts, (uint32_t)n, sc, 1u);
     return cudaGetLastError();
 }
+
+// ---------------------------------------------------------------------------
+// Entry point for callers that cannot allocate GPU memory.
+//
+// Some callers of a PoH verifier are not allowed to call cudaMalloc: a
+// validator pipeline whose GPU memory is owned by a pooling allocator with a
+// fixed budget, or one that must not take the device-wide synchronisation
+// that cudaMalloc / cudaFree can cause in the middle of other streams' work.
+// For them the ragged-batch scratch (entry order, bucket counts, queue head)
+// lives in this file-scope device array instead of a caller workspace.  The
+// array is part of the library image: every GPU that loads the library holds
+// it until the process exits.
+#include <cstdio>
+#include <mutex>
+
+namespace {
+
+constexpr uint64_t kStaticMaxEntries = 262144;   // 1 MiB of entry order + the header
+
+static __device__ __align__(256) uint8_t g_poh_static_scratch[sizeof(PohBatchScratch) + 4 * kStaticMaxEntries];
+
+constexpr int kStaticMaxDevices = 64;
+std::mutex g_static_mu;
+void* g_static_ptr[kStaticMaxDevices];   // device address of the array, per device
+int g_static_sms[kStaticMaxDevices];
+
+}  // namespace
+
+extern "C" int gb300_poh_verify_batch_static(uint8_t* hashes, const uint64_t* num_hashes, uint64_t num_elems,
+                                             void* stream) {
+    if (num_elems == 0) return 0;
+    if (num_elems > kStaticMaxEntries) {
+        fprintf(stderr,
+                "gb300_poh_verify_batch_static: %llu entries exceed the static scratch limit of %llu entries\n",
+                (unsigned long long)num_elems, (unsigned long long)kStaticMaxEntries);
+        return (int)cudaErrorInvalidValue;
+    }
+    if ((reinterpret_cast<uintptr_t>(hashes) & 15u) || (reinterpret_cast<uintptr_t>(num_hashes) & 7u))
+        return (int)cudaErrorMisalignedAddress;
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return (int)e;
+    if (dev < 0 || dev >= kStaticMaxDevices) return (int)cudaErrorInvalidDevice;
+    void* scratch = nullptr;
+    int sms = 0;
+    {
+        // once per device, with that device current: the array's device
+        // address (the host-side symbol is only a stand-in) and the SM count
+        std::lock_guard<std::mutex> lk(g_static_mu);
+        if (!g_static_ptr[dev]) {
+            void* p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_poh_static_scratch);
+            if (e != cudaSuccess) return (int)e;
+            int n = 0;
+            e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+            if (e != cudaSuccess) return (int)e;
+            g_static_sms[dev] = n > 0 ? n : 1;
+            g_static_ptr[dev] = p;
+        }
+        scratch = g_static_ptr[dev];
+        sms = g_static_sms[dev];
+    }
+    // The array keeps the previous call's contents; launch_poh_batch clears
+    // the header (bucket counts, cursors, queue head) on every call and
+    // rewrites the entry order in full.  One warp per SM sub-partition, the
+    // shape the autotuner picks on GB300.
+    return (int)launch_poh_batch(hashes, num_hashes, num_elems, scratch, 4 * sms, static_cast<cudaStream_t>(stream));
+}
