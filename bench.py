@@ -386,6 +386,171 @@ def bench_ragged_sigs(lib, torch):
             "results_identical_per_call_vs_batched": True, "valid_class_all_accepted": valid_ok}
 
 
+def _pct(xs, q):
+    return float(np.percentile(np.asarray(xs), q)) if len(xs) else None
+
+
+def bench_serving(lib, levels=(0.1, 0.25, 0.5, 0.8, 1.0, 1.2), duration_s=1.0):
+    """Open-loop Poisson arrivals of a request mix (80% verify batches of the
+    ragged-batch size/message/adversarial distributions, 15% PoH batches of
+    64 entries with num_hashes log-uniform in 1..1e6, 5% sign batches of 128
+    packets) into the served loop, at fractions of its measured peak; every
+    result checked against the same request run alone."""
+    import queue
+    import threading
+    import workloads
+    from cuda_crypt import JOB_SIGN, JOB_VERIFY, Server
+    rng = np.random.default_rng(9)
+    rs = workloads.ragged_sigs(lib.create_keypairs, lib.sign_many, n_batches=40, seed=6)
+    vpool, spool = rs.verify, rs.sign[:40]
+    ppool = [workloads.poh_ragged(n=64, max_hashes=1_000_000, seed=100 + k) for k in range(8)]
+    for sp in vpool + spool:
+        for b in sp.batches:
+            lib.host_register(b)
+    alone_v = [lib.verify_many(sp) for sp in vpool]
+    alone_s = [lib.sign_many(sp) for sp in spool]
+    alone_p = []
+    for h, c in ppool:
+        b = h.ravel().copy()
+        lib.poh_verify_many(b, c)
+        alone_p.append(b)
+
+    def draw(n):
+        out = []
+        for _ in range(n):
+            u = rng.random()
+            if u < 0.80:
+                out.append(("v", int(rng.integers(len(vpool)))))
+            elif u < 0.95:
+                out.append(("p", int(rng.integers(len(ppool)))))
+            else:
+                out.append(("s", int(rng.integers(len(spool)))))
+        return out
+
+    def items(kind, k):
+        return vpool[k].total_signatures if kind == "v" else spool[k].total_signatures if kind == "s" else 0
+
+    def submit(srv, kind, k):
+        if kind == "v":
+            return srv.submit_sigs(vpool[k], JOB_VERIFY)
+        if kind == "s":
+            return srv.submit_sigs(spool[k], JOB_SIGN)
+        h, c = ppool[k]
+        out = h.ravel().copy()
+        return srv.submit_poh(out, c), out
+
+    def check(kind, k, out):
+        exp = alone_v[k] if kind == "v" else alone_s[k] if kind == "s" else alone_p[k]
+        return np.array_equal(out, exp)
+
+    srv = Server(lib)
+    ok_all = True
+    try:
+        # peak: a burst of the mix, time until its signature requests are done
+        burst = draw(200)
+        t0 = time.perf_counter()
+        subs = [(kind, k) + tuple(submit(srv, kind, k)) for kind, k in burst]
+        last_sig = t0
+        for kind, k, t, out in subs:
+            if kind != "p":
+                srv.wait(t, release=False)
+                last_sig = max(last_sig, time.perf_counter())
+        for kind, k, t, out in subs:
+            srv.wait(t)
+            ok_all &= check(kind, k, out)
+        peak_rps = len(burst) / (last_sig - t0)
+        peak_items = sum(items(kd, k) for kd, k in burst) / (last_sig - t0)
+        rows = []
+        for lv in levels:
+            lam = lv * peak_rps
+            n = max(30, int(lam * duration_s))
+            arrivals = np.cumsum(rng.exponential(1.0 / lam, n))
+            reqs = draw(n)
+            start = time.perf_counter()
+            subs = []
+            for (kind, k), ta in zip(reqs, arrivals):
+                dt = start + ta - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                subs.append((kind, k) + tuple(submit(srv, kind, k)))
+            lat = {"v": [], "s": [], "p": []}
+            t_first, t_last, sig_items = None, None, 0
+            for kind, k, t, out in subs:
+                srv.wait(t, release=False)
+                a, b = srv.times_ns(t)
+                lat[kind].append((b - a) * 1e-9)
+                ok_all &= check(kind, k, out)
+                if kind != "p":
+                    t_first = a if t_first is None else min(t_first, a)
+                    t_last = b if t_last is None else max(t_last, b)
+                    sig_items += items(kind, k)
+                srv.release(t)
+            sig_lat = lat["v"] + lat["s"]
+            rows.append({"offered_fraction_of_peak": lv, "offered_requests_per_s": lam, "requests": n,
+                         "sig_items_per_s": sig_items / max(1e-9, (t_last - t_first) * 1e-9),
+                         "sig_latency_ms": {"p50": _pct(sig_lat, 50) * 1e3, "p99": _pct(sig_lat, 99) * 1e3,
+                                            "p99.9": _pct(sig_lat, 99.9) * 1e3},
+                         "verify_latency_ms_p99": (_pct(lat["v"], 99) or 0) * 1e3,
+                         "poh_latency_ms": {"p50": (_pct(lat["p"], 50) or 0) * 1e3,
+                                            "p99": (_pct(lat["p"], 99) or 0) * 1e3}})
+        stats = srv.stats()
+    finally:
+        srv.close()
+    # the plain per-request calls at 80% of the served peak, 4 caller threads
+    lam = 0.8 * peak_rps
+    n = max(30, int(lam * duration_s))
+    arrivals = np.cumsum(rng.exponential(1.0 / lam, n))
+    reqs = draw(n)
+    q = queue.Queue()
+    lat = {"v": [], "s": [], "p": []}
+    lk = threading.Lock()
+
+    def worker():
+        while True:
+            item = q.get()
+            if item is None:
+                return
+            kind, k, t_arr = item
+            if kind == "v":
+                out = lib.verify_many(vpool[k])
+            elif kind == "s":
+                out = lib.sign_many(spool[k])
+            else:
+                h, c = ppool[k]
+                out = h.ravel().copy()
+                lib.poh_verify_many(out, c)
+            with lk:
+                lat[kind].append(time.perf_counter() - t_arr)
+    ths = [threading.Thread(target=worker) for _ in range(4)]
+    for th in ths:
+        th.start()
+    start = time.perf_counter()
+    for (kind, k), ta in zip(reqs, arrivals):
+        dt = start + ta - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        q.put((kind, k, time.perf_counter()))
+    for _ in ths:
+        q.put(None)
+    for th in ths:
+        th.join()
+    plain_sig = lat["v"] + lat["s"]
+    for sp in vpool + spool:
+        for b in sp.batches:
+            lib.host_unregister(b)
+    return {"config": {"workload": "open-loop Poisson arrivals; mix 80% verify batches (ragged sizes 1..8192 "
+                                   "packets, 0..1232-B messages, adversarial classes), 15% PoH batches (64 entries, "
+                                   "num_hashes log-uniform 1..1e6), 5% sign batches (128 packets)",
+                       "device_memory_cap_bytes": 8 << 30, "request_pool": {"verify": len(vpool), "sign": len(spool),
+                                                                           "poh": len(ppool)}},
+            "peak_requests_per_s": peak_rps, "peak_sig_items_per_s": peak_items, "levels": rows,
+            "plain_per_request_at_0.8_peak": {"sig_latency_ms": {"p50": _pct(plain_sig, 50) * 1e3,
+                                                                 "p99": _pct(plain_sig, 99) * 1e3,
+                                                                 "p99.9": _pct(plain_sig, 99.9) * 1e3},
+                                              "caller_threads": 4, "requests": n},
+            "results_identical_alone_and_in_mix": bool(ok_all), "server_stats": stats}
+
+
 def cpu_poh(h0, cnt, nthreads, sample_entries):
     from oracle.oracle import get_oracle
     o = get_oracle()
@@ -493,6 +658,8 @@ def run_ours(args):
     if not args.skip_ragged:
         line["poh_ragged"] = bench_poh_ragged(lib, torch, steps=2)
         line["ragged_sigs"] = bench_ragged_sigs(lib, torch)
+    if not args.skip_serving:
+        line["serving"] = bench_serving(lib)
     line["autotuner"] = lib.tuning()
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -587,6 +754,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--case", default=None, help="run one small kernel case (for profiling) and exit")
     ap.add_argument("--skip-ragged", action="store_true", help="skip the ragged PoH / signature batch sections")
+    ap.add_argument("--skip-serving", action="store_true", help="skip the served-loop section")
     args = ap.parse_args()
     if args.case:
         run_case(args.case)

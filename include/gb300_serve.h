@@ -1,0 +1,73 @@
+/*
+ * gb300_serve.h -- served request loop of libcuda-crypt.so (no counterpart
+ * in the reference, which only has the synchronous one-batch calls).
+ *
+ * A server owns one GPU (the device current at creation) and a dispatcher
+ * thread.  Requests -- an Ed25519 verify or sign job, or a PoH batch -- are
+ * queued by any thread and admitted as launch slots and device memory free
+ * up (device memory held by in-flight requests stays below the configured
+ * cap).  Signature requests that arrive while earlier ones are on the GPU
+ * are merged into the next persistent launch (continuous batching) on
+ * high-priority streams; PoH requests run on a low-priority stream so a long
+ * chain does not hold up signature work.  Each request's results are exactly
+ * those of the corresponding one-call entry point.
+ *
+ * The caller's buffers must stay valid, and its outputs untouched, until
+ * the request is complete.  Page-locked (cuda_host_register) packet buffers
+ * are copied to the GPU directly; others go through the server's staging.
+ */
+#ifndef GB300_CRYPT_SERVE_H
+#define GB300_CRYPT_SERVE_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include "ed25519.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gb300_server gb300_server;
+
+typedef struct {
+    uint64_t device_memory_cap;      /* bytes in flight on the GPU; 0 = 8 GiB */
+    uint32_t sig_slots;              /* concurrent signature launches; 0 = 3 */
+    uint32_t poh_slots;              /* concurrent PoH launches; 0 = 2 */
+    uint32_t max_items_per_launch;   /* signatures merged into one launch; 0 = 65536 */
+} gb300_server_config;
+
+/* Creates a server on the current device (cfg may be NULL); NULL on failure. */
+gb300_server* gb300_server_create(const gb300_server_config* cfg);
+
+/* Finishes every admitted and queued request, then stops. */
+void gb300_server_destroy(gb300_server* s);
+
+/* Queues one verify (job->kind 0) or sign (kind 1) job; returns a ticket
+ * (> 0) or 0 when the job is invalid or alone exceeds the memory cap. */
+uint64_t gb300_server_submit_sigs(gb300_server* s, const gb300_sig_job* job);
+
+/* Queues a PoH batch (in place on hashes, as poh_verify_many); ticket or 0. */
+uint64_t gb300_server_submit_poh(gb300_server* s, uint8_t* hashes, const uint64_t* num_hashes, size_t num_elems);
+
+/* 1 when the request is complete, 0 while pending, negative cudaError_t on
+ * failure (the outputs are then zero). */
+int gb300_server_poll(gb300_server* s, uint64_t ticket);
+
+/* Blocks until completion or timeout_ms (< 0: no limit); returns as poll. */
+int gb300_server_wait(gb300_server* s, uint64_t ticket, int timeout_ms);
+
+/* Forgets a completed ticket (frees its bookkeeping). */
+void gb300_server_release(gb300_server* s, uint64_t ticket);
+
+/* Submission and completion times of a ticket (steady clock, ns; done_ns
+ * is -1 while pending); returns 1 when complete, 0 while pending. */
+int gb300_server_times(gb300_server* s, uint64_t ticket, int64_t* submit_ns, int64_t* done_ns);
+
+/* Counters as a JSON object; returns the length written. */
+int gb300_server_stats(gb300_server* s, char* buf, size_t len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -27,10 +27,15 @@
 #include "poh_verify.h"
 #include "kernels.h"
 #include "tables.cuh"
+#include "host_buffers.h"
 
 #include <functional>
 
 namespace {
+
+using gb300::DevBuf;
+using gb300::HostBuf;
+using gb300::round_up;
 
 constexpr int kMaxGpus = 8;
 constexpr int kQueues = 8;
@@ -45,52 +50,6 @@ thread_local int t_last_error = 0;
             fflush(stdout);                            \
         }                                              \
     } while (0)
-
-size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
-
-struct DevBuf {
-    void* p = nullptr;
-    size_t cap = 0;
-    cudaError_t ensure(size_t bytes) {
-        if (p && bytes <= cap) return cudaSuccess;
-        release();
-        size_t want = round_up(bytes < 4096 ? 4096 : bytes + bytes / 4, 4096);
-        cudaError_t e = cudaMalloc(&p, want);
-        if (e != cudaSuccess) {
-            p = nullptr;
-            return e;
-        }
-        cap = want;
-        return cudaSuccess;
-    }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-    }
-};
-
-struct HostBuf {
-    void* p = nullptr;
-    size_t cap = 0;
-    cudaError_t ensure(size_t bytes) {
-        if (p && bytes <= cap) return cudaSuccess;
-        release();
-        size_t want = round_up(bytes < 4096 ? 4096 : bytes + bytes / 4, 4096);
-        cudaError_t e = cudaMallocHost(&p, want);
-        if (e != cudaSuccess) {
-            p = nullptr;
-            return e;
-        }
-        cap = want;
-        return cudaSuccess;
-    }
-    void release() {
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        cap = 0;
-    }
-};
 
 // A captured launch sequence, replayed while its key (sizes, buffer
 // addresses, launch shape) stays the same.
@@ -515,6 +474,22 @@ void sig_many(bool sign, const gpu_Elems* elems, uint32_t num_elems, uint32_t me
 }
 
 }  // namespace
+
+bool crypt_device_info(int dev, CryptDeviceInfo* out) {
+    Device* D = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        if (!init_locked() || dev < 0 || dev >= g_num_gpus) return false;
+        D = &g_dev[dev];
+    }
+    const Tuning& T = tuning_for(*D);
+    out->tables = D->tables;
+    out->sms = D->sms;
+    out->sig_threads = T.sig_threads;
+    out->sig_blocks_per_sm = T.sig_blocks_per_sm;
+    out->poh_warps = 4 * D->sms * T.poh_warps_per_smsp;
+    return true;
+}
 
 extern "C" {
 

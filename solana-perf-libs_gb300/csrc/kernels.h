@@ -59,3 +59,14 @@ struct SigWork {
     uint32_t* next;          // queue head, device word (reset by the launch)
 };
 cudaError_t launch_sig_batch(const SigWork& w, int threads, int blocks_per_sm, int sms, cudaStream_t s);
+
+// Per-device state the served loop (server.cu) needs from the pool
+// (crypt_api.cu): device tables and the autotuner's launch shapes.
+struct CryptDeviceInfo {
+    const CurveTables* tables;
+    int sms;
+    int sig_threads;
+    int sig_blocks_per_sm;
+    int poh_warps;          // resident warps for the persistent PoH kernel
+};
+bool crypt_device_info(int dev, CryptDeviceInfo* out);

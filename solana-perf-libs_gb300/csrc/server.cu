@@ -1,0 +1,480 @@
+// Served request loop (include/gb300_serve.h): continuous batching of
+// Ed25519 verify/sign jobs and PoH batches on one GPU.
+//
+// One dispatcher thread per server:
+//   * completion: for every busy slot whose event has fired, copy each
+//     request's results out of the slot's page-locked output, mark its ticket
+//     done and return the slot's device bytes to the admission budget;
+//   * admission: while a signature slot is free, take queued verify/sign
+//     jobs in arrival order until the launch's item cap or the memory budget
+//     would be exceeded, and run them as ONE persistent launch (the mixed
+//     kernel of sig_batch.cu) on that slot's high-priority stream; likewise
+//     PoH batches on low-priority streams (persistent PoH kernel);
+//   * sleep on a condition variable when there is nothing to do (woken by
+//     submissions; polls the GPU every 20 us while work is in flight).
+// Slot buffers (device rings and page-locked staging) are grow-only and stay
+// resident, as do the basepoint tables.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <condition_variable>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "ed25519.h"
+#include "gb300_serve.h"
+#include "host_buffers.h"
+#include "kernels.h"
+#include "tables.cuh"
+
+namespace {
+
+using gb300::DevBuf;
+using gb300::HostBuf;
+using gb300::round_up;
+
+bool page_locked(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+struct Req {
+    uint64_t ticket = 0;
+    int kind = 0;                 // 0 verify, 1 sign, 2 poh
+    gb300_sig_job job{};
+    uint8_t* hashes = nullptr;
+    const uint64_t* counts = nullptr;
+    uint64_t n = 0;               // items (signatures or entries)
+    uint64_t bytes = 0;           // device bytes while in flight
+};
+
+struct Slot {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    bool busy = false;
+    int kind = 0;                 // 0 signatures, 2 PoH
+    DevBuf d_data, d_index, d_out, d_scratch;
+    HostBuf h_stage, h_out;
+    std::vector<Req> reqs;
+    uint64_t bytes = 0;
+    uint64_t nv = 0, ns = 0, sig_out_off = 0, poh_n = 0;
+    cudaError_t err = cudaSuccess;
+};
+
+}  // namespace
+
+struct gb300_server {
+    int dev = -1;
+    CryptDeviceInfo info{};
+    uint64_t cap = 0, in_use = 0;
+    uint32_t max_items = 0;
+    std::vector<Slot> sig_slots, poh_slots;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<Req> pending_sig, pending_poh;
+    std::unordered_map<uint64_t, int> status;   // 0 pending, 1 done, < 0 error
+    std::unordered_map<uint64_t, std::pair<int64_t, int64_t>> times;   // submit, completion (steady ns)
+    uint64_t next_ticket = 1;
+    bool stop = false;
+    std::thread worker;
+    // counters
+    uint64_t launches_sig = 0, launches_poh = 0, requests_done = 0, merged_max = 0, items_done = 0;
+};
+
+namespace {
+
+int64_t now_ns() {
+    return std::chrono::duration_cast<std::chrono::nanoseconds>(
+               std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+uint64_t sig_bytes(const gb300_sig_job& j) {
+    return j.packets_len + 16ull * j.num + (j.kind == 0 ? j.num : 64ull * j.num) + 64;
+}
+
+// Stage and launch the requests in S.reqs (signature jobs) on S.stream.
+cudaError_t launch_sigs(gb300_server* sv, Slot& S) {
+    uint64_t nv = 0, ns = 0, total = 0;
+    bool locked = true;
+    for (auto& r : S.reqs) {
+        (r.kind == 0 ? nv : ns) += r.n;
+        total += r.job.packets_len;
+        if (r.job.packets_len && locked) locked = page_locked(r.job.packets);
+    }
+    S.nv = nv;
+    S.ns = ns;
+    S.sig_out_off = round_up(nv, 64);
+    const size_t idx_bytes = 16ull * (nv + ns), out_bytes = S.sig_out_off + 64ull * ns;
+    const size_t pk_off = round_up(idx_bytes, 256);
+    cudaError_t e;
+    if ((e = S.d_data.ensure(total + 16)) != cudaSuccess) return e;
+    if ((e = S.d_index.ensure(idx_bytes)) != cudaSuccess) return e;
+    if ((e = S.d_out.ensure(out_bytes)) != cudaSuccess) return e;
+    if ((e = S.d_scratch.ensure(256)) != cudaSuccess) return e;
+    if ((e = S.h_stage.ensure(pk_off + (locked ? 0 : total))) != cudaSuccess) return e;
+    if ((e = S.h_out.ensure(out_bytes)) != cudaSuccess) return e;
+    uint32_t* hv = static_cast<uint32_t*>(S.h_stage.p);
+    uint32_t* hs = hv + 4 * nv;
+    uint8_t* img = static_cast<uint8_t*>(S.h_stage.p) + pk_off;
+    uint8_t* dpk = static_cast<uint8_t*>(S.d_data.p);
+    uint64_t base = 0, iv = 0, is = 0;
+    for (auto& r : S.reqs) {
+        const gb300_sig_job& J = r.job;
+        uint32_t* h = r.kind == 0 ? hv : hs;
+        const uint64_t cnt = r.kind == 0 ? nv : ns;
+        uint64_t& pos = r.kind == 0 ? iv : is;
+        for (uint32_t i = 0; i < J.num; i++) {
+            const uint64_t m = J.message_lens[i], po = J.public_key_offsets[i], ko = J.key_offsets[i],
+                           mo = J.message_start_offsets[i];
+            const bool ok = po + 32 <= J.packets_len && ko + 64 <= J.packets_len && mo + m <= J.packets_len;
+            h[pos + i] = ok ? (uint32_t)m : 0xffffffffu;
+            h[cnt + pos + i] = ok ? (uint32_t)(base + po) : 0u;
+            h[2 * cnt + pos + i] = ok ? (uint32_t)(base + ko) : 0u;
+            h[3 * cnt + pos + i] = ok ? (uint32_t)(base + mo) : 0u;
+        }
+        if (J.packets_len) {
+            if (locked) {
+                e = cudaMemcpyAsync(dpk + base, J.packets, J.packets_len, cudaMemcpyHostToDevice, S.stream);
+                if (e != cudaSuccess) return e;
+            } else {
+                memcpy(img + base, J.packets, J.packets_len);
+            }
+        }
+        pos += J.num;
+        base += J.packets_len;
+    }
+    if ((e = cudaMemcpyAsync(S.d_index.p, S.h_stage.p, idx_bytes, cudaMemcpyHostToDevice, S.stream)) != cudaSuccess)
+        return e;
+    if (!locked && total && (e = cudaMemcpyAsync(dpk, img, total, cudaMemcpyHostToDevice, S.stream)) != cudaSuccess)
+        return e;
+    const uint32_t* dv = static_cast<const uint32_t*>(S.d_index.p);
+    const uint32_t* ds = dv + 4 * nv;
+    uint8_t* dout = static_cast<uint8_t*>(S.d_out.p);
+    SigWork w;
+    w.v = SigBatch{dpk, total, dv, dv + nv, dv + 2 * nv, dv + 3 * nv, (uint32_t)nv, dout, sv->info.tables};
+    w.s = SigBatch{dpk, total, ds, ds + ns, ds + 2 * ns, ds + 3 * ns, (uint32_t)ns, dout + S.sig_out_off,
+                   sv->info.tables};
+    w.sign_base = (uint32_t)((nv + 31) / 32 * 32);
+    w.total_chunks = (uint32_t)((w.sign_base + ns + 31) / 32);
+    w.next = static_cast<uint32_t*>(S.d_scratch.p);
+    if ((e = launch_sig_batch(w, sv->info.sig_threads, sv->info.sig_blocks_per_sm, sv->info.sms, S.stream)) !=
+        cudaSuccess)
+        return e;
+    if ((e = cudaMemcpyAsync(S.h_out.p, dout, out_bytes, cudaMemcpyDeviceToHost, S.stream)) != cudaSuccess) return e;
+    return cudaEventRecord(S.done, S.stream);
+}
+
+cudaError_t launch_pohs(gb300_server* sv, Slot& S) {
+    uint64_t n = 0;
+    for (auto& r : S.reqs) n += r.n;
+    S.poh_n = n;
+    const size_t hb = 32ull * n, cb = 8ull * n;
+    cudaError_t e;
+    if ((e = S.d_data.ensure(hb + cb)) != cudaSuccess) return e;
+    if ((e = S.d_scratch.ensure(poh_batch_workspace_size(n))) != cudaSuccess) return e;
+    if ((e = S.h_stage.ensure(hb + cb)) != cudaSuccess) return e;
+    uint8_t* st = static_cast<uint8_t*>(S.h_stage.p);
+    uint64_t pos = 0;
+    for (auto& r : S.reqs) {
+        memcpy(st + 32 * pos, r.hashes, 32ull * r.n);
+        memcpy(st + hb + 8 * pos, r.counts, 8ull * r.n);
+        pos += r.n;
+    }
+    uint8_t* d = static_cast<uint8_t*>(S.d_data.p);
+    if ((e = cudaMemcpyAsync(d, st, hb + cb, cudaMemcpyHostToDevice, S.stream)) != cudaSuccess) return e;
+    if ((e = launch_poh_batch(d, reinterpret_cast<const uint64_t*>(d + hb), n, S.d_scratch.p, sv->info.poh_warps,
+                              S.stream)) != cudaSuccess)
+        return e;
+    if ((e = cudaMemcpyAsync(st, d, hb, cudaMemcpyDeviceToHost, S.stream)) != cudaSuccess) return e;
+    return cudaEventRecord(S.done, S.stream);
+}
+
+// Results of a finished slot back to the callers (dispatcher thread, no lock held).
+void deliver(Slot& S) {
+    if (S.kind == 0) {
+        const uint8_t* ho = static_cast<const uint8_t*>(S.h_out.p);
+        uint64_t ov = 0, os = 0;
+        for (auto& r : S.reqs) {
+            if (r.kind == 0) {
+                if (S.err == cudaSuccess) memcpy(r.job.out, ho + ov, r.n);
+                else memset(r.job.out, 0, r.n);
+                ov += r.n;
+            } else {
+                if (S.err == cudaSuccess) memcpy(r.job.out, ho + S.sig_out_off + 64 * os, 64ull * r.n);
+                else memset(r.job.out, 0, 64ull * r.n);
+                os += r.n;
+            }
+        }
+    } else if (S.err == cudaSuccess) {
+        const uint8_t* st = static_cast<const uint8_t*>(S.h_stage.p);
+        uint64_t pos = 0;
+        for (auto& r : S.reqs) {
+            memcpy(r.hashes, st + 32 * pos, 32ull * r.n);
+            pos += r.n;
+        }
+    }
+}
+
+void dispatcher(gb300_server* sv) {
+    cudaSetDevice(sv->dev);
+    std::unique_lock<std::mutex> lk(sv->mu);
+    for (;;) {
+        // ---- completions ----
+        bool any_busy = false;
+        for (auto* slots : {&sv->sig_slots, &sv->poh_slots}) {
+            for (auto& S : *slots) {
+                if (!S.busy) continue;
+                cudaError_t q = S.err != cudaSuccess ? cudaSuccess : cudaEventQuery(S.done);
+                if (q == cudaErrorNotReady) {
+                    any_busy = true;
+                    continue;
+                }
+                if (q != cudaSuccess && S.err == cudaSuccess) S.err = q;
+                lk.unlock();
+                // a launch that failed part-way may still have copies queued:
+                // drain the stream before the slot's buffers are reused
+                cudaStreamSynchronize(S.stream);
+                cudaGetLastError();
+                deliver(S);
+                lk.lock();
+                const int64_t t_done = now_ns();
+                for (auto& r : S.reqs) {
+                    sv->times[r.ticket].second = t_done;
+                    sv->status[r.ticket] = S.err == cudaSuccess ? 1 : -(int)S.err;
+                    sv->requests_done++;
+                    sv->items_done += r.n;
+                }
+                sv->in_use -= S.bytes;
+                S.reqs.clear();
+                S.bytes = 0;
+                S.busy = false;
+                S.err = cudaSuccess;
+                sv->cv_done.notify_all();
+            }
+        }
+        // ---- admission ----
+        bool launched = false;
+        for (auto& S : sv->sig_slots) {
+            if (S.busy || sv->pending_sig.empty()) continue;
+            uint64_t items = 0, bytes = 0;
+            while (!sv->pending_sig.empty()) {
+                const Req& r = sv->pending_sig.front();
+                if (!S.reqs.empty() && (items + r.n > sv->max_items || sv->in_use + bytes + r.bytes > sv->cap)) break;
+                if (S.reqs.empty() && sv->in_use + r.bytes > sv->cap) break;   // wait for memory
+                items += r.n;
+                bytes += r.bytes;
+                S.reqs.push_back(r);
+                sv->pending_sig.pop_front();
+            }
+            if (S.reqs.empty()) continue;
+            S.busy = true;
+            S.kind = 0;
+            S.bytes = bytes;
+            sv->in_use += bytes;
+            sv->launches_sig++;
+            if (S.reqs.size() > sv->merged_max) sv->merged_max = S.reqs.size();
+            lk.unlock();
+            S.err = launch_sigs(sv, S);
+            lk.lock();
+            launched = true;
+        }
+        for (auto& S : sv->poh_slots) {
+            if (S.busy || sv->pending_poh.empty()) continue;
+            uint64_t bytes = 0;
+            while (!sv->pending_poh.empty()) {
+                const Req& r = sv->pending_poh.front();
+                if (sv->in_use + bytes + r.bytes > sv->cap) break;
+                bytes += r.bytes;
+                S.reqs.push_back(r);
+                sv->pending_poh.pop_front();
+            }
+            if (S.reqs.empty()) continue;
+            S.busy = true;
+            S.kind = 2;
+            S.bytes = bytes;
+            sv->in_use += bytes;
+            sv->launches_poh++;
+            lk.unlock();
+            S.err = launch_pohs(sv, S);
+            lk.lock();
+            launched = true;
+        }
+        if (launched) continue;
+        bool busy = false;
+        for (auto* slots : {&sv->sig_slots, &sv->poh_slots})
+            for (auto& S : *slots) busy |= S.busy;
+        if (sv->stop && !busy && sv->pending_sig.empty() && sv->pending_poh.empty()) break;
+        if (busy || any_busy)
+            sv->cv_work.wait_for(lk, std::chrono::microseconds(20));
+        else
+            sv->cv_work.wait(lk);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+gb300_server* gb300_server_create(const gb300_server_config* cfg) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    auto* sv = new gb300_server();
+    sv->dev = dev;
+    if (!crypt_device_info(dev, &sv->info)) {
+        delete sv;
+        return nullptr;
+    }
+    sv->cap = cfg && cfg->device_memory_cap ? cfg->device_memory_cap : (8ull << 30);
+    sv->max_items = cfg && cfg->max_items_per_launch ? cfg->max_items_per_launch : 65536u;
+    const uint32_t nsig = cfg && cfg->sig_slots ? cfg->sig_slots : 3u;
+    const uint32_t npoh = cfg && cfg->poh_slots ? cfg->poh_slots : 2u;
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);   // hi is the numerically smaller, higher priority
+    sv->sig_slots.resize(nsig);
+    sv->poh_slots.resize(npoh);
+    bool ok = true;
+    for (auto& S : sv->sig_slots)
+        ok = ok && cudaStreamCreateWithPriority(&S.stream, cudaStreamNonBlocking, hi) == cudaSuccess &&
+             cudaEventCreateWithFlags(&S.done, cudaEventDisableTiming) == cudaSuccess;
+    for (auto& S : sv->poh_slots)
+        ok = ok && cudaStreamCreateWithPriority(&S.stream, cudaStreamNonBlocking, lo) == cudaSuccess &&
+             cudaEventCreateWithFlags(&S.done, cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        gb300_server_destroy(sv);
+        return nullptr;
+    }
+    sv->worker = std::thread(dispatcher, sv);
+    return sv;
+}
+
+void gb300_server_destroy(gb300_server* sv) {
+    if (!sv) return;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->stop = true;
+    }
+    sv->cv_work.notify_all();
+    if (sv->worker.joinable()) sv->worker.join();
+    int prev = -1;
+    cudaGetDevice(&prev);
+    cudaSetDevice(sv->dev);
+    for (auto* slots : {&sv->sig_slots, &sv->poh_slots})
+        for (auto& S : *slots) {
+            if (S.stream) cudaStreamSynchronize(S.stream);
+            S.d_data.release();
+            S.d_index.release();
+            S.d_out.release();
+            S.d_scratch.release();
+            S.h_stage.release();
+            S.h_out.release();
+            if (S.done) cudaEventDestroy(S.done);
+            if (S.stream) cudaStreamDestroy(S.stream);
+        }
+    if (prev >= 0) cudaSetDevice(prev);
+    delete sv;
+}
+
+uint64_t gb300_server_submit_sigs(gb300_server* sv, const gb300_sig_job* job) {
+    if (!sv || !job || job->kind > 1 || job->num == 0 || !job->out || !job->message_lens ||
+        !job->public_key_offsets || !job->key_offsets || !job->message_start_offsets ||
+        (job->packets_len && !job->packets) || job->packets_len >= 0xfffffff0ull)
+        return 0;
+    Req r;
+    r.kind = (int)job->kind;
+    r.job = *job;
+    r.n = job->num;
+    r.bytes = sig_bytes(*job);
+    if (r.bytes > sv->cap || r.n > sv->max_items) return 0;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    r.ticket = sv->next_ticket++;
+    sv->status[r.ticket] = 0;
+    sv->times[r.ticket] = {now_ns(), -1};
+    sv->pending_sig.push_back(r);
+    sv->cv_work.notify_one();
+    return r.ticket;
+}
+
+uint64_t gb300_server_submit_poh(gb300_server* sv, uint8_t* hashes, const uint64_t* num_hashes, size_t num_elems) {
+    if (!sv || !hashes || !num_hashes || num_elems == 0 || num_elems > 0x7fffffffull) return 0;
+    Req r;
+    r.kind = 2;
+    r.hashes = hashes;
+    r.counts = num_hashes;
+    r.n = num_elems;
+    r.bytes = 40ull * num_elems + poh_batch_workspace_size(num_elems);
+    if (r.bytes > sv->cap) return 0;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    r.ticket = sv->next_ticket++;
+    sv->status[r.ticket] = 0;
+    sv->times[r.ticket] = {now_ns(), -1};
+    sv->pending_poh.push_back(r);
+    sv->cv_work.notify_one();
+    return r.ticket;
+}
+
+int gb300_server_poll(gb300_server* sv, uint64_t ticket) {
+    if (!sv) return -(int)cudaErrorInvalidValue;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    auto it = sv->status.find(ticket);
+    return it == sv->status.end() ? -(int)cudaErrorInvalidValue : it->second;
+}
+
+int gb300_server_wait(gb300_server* sv, uint64_t ticket, int timeout_ms) {
+    if (!sv) return -(int)cudaErrorInvalidValue;
+    std::unique_lock<std::mutex> lk(sv->mu);
+    auto done = [&]() {
+        auto it = sv->status.find(ticket);
+        return it == sv->status.end() || it->second != 0;
+    };
+    if (timeout_ms < 0)
+        sv->cv_done.wait(lk, done);
+    else
+        sv->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), done);
+    auto it = sv->status.find(ticket);
+    return it == sv->status.end() ? -(int)cudaErrorInvalidValue : it->second;
+}
+
+void gb300_server_release(gb300_server* sv, uint64_t ticket) {
+    if (!sv) return;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    auto it = sv->status.find(ticket);
+    if (it != sv->status.end() && it->second != 0) {
+        sv->status.erase(it);
+        sv->times.erase(ticket);
+    }
+}
+
+int gb300_server_times(gb300_server* sv, uint64_t ticket, int64_t* submit_ns, int64_t* done_ns) {
+    if (!sv) return -(int)cudaErrorInvalidValue;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    auto it = sv->times.find(ticket);
+    if (it == sv->times.end()) return -(int)cudaErrorInvalidValue;
+    if (submit_ns) *submit_ns = it->second.first;
+    if (done_ns) *done_ns = it->second.second;
+    return it->second.second >= 0 ? 1 : 0;
+}
+
+int gb300_server_stats(gb300_server* sv, char* buf, size_t len) {
+    if (!sv || !buf || len == 0) return 0;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    int n = snprintf(buf, len,
+                     "{\"device\": %d, \"launches_sig\": %llu, \"launches_poh\": %llu, \"requests_done\": %llu, "
+                     "\"items_done\": %llu, \"max_requests_merged\": %llu, \"pending_sig\": %zu, "
+                     "\"pending_poh\": %zu, \"device_bytes_in_flight\": %llu, \"device_memory_cap\": %llu}",
+                     sv->dev, (unsigned long long)sv->launches_sig, (unsigned long long)sv->launches_poh,
+                     (unsigned long long)sv->requests_done, (unsigned long long)sv->items_done,
+                     (unsigned long long)sv->merged_max, sv->pending_sig.size(), sv->pending_poh.size(),
+                     (unsigned long long)sv->in_use, (unsigned long long)sv->cap);
+    return n < 0 ? 0 : (n < (int)len ? n : (int)len - 1);
+}
+
+}  // extern "C"

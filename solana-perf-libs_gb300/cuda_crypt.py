@@ -294,6 +294,102 @@ class CudaCrypt:
             raise RuntimeError(f"gb300_poh_verify_device: cudaError {rc}")
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("device_memory_cap", ctypes.c_uint64), ("sig_slots", ctypes.c_uint32),
+                ("poh_slots", ctypes.c_uint32), ("max_items_per_launch", ctypes.c_uint32)]
+
+
+class Server:
+    """The served request loop (include/gb300_serve.h) on the current GPU."""
+
+    def __init__(self, lib: "CudaCrypt", device_memory_cap: int = 0, sig_slots: int = 0, poh_slots: int = 0,
+                 max_items_per_launch: int = 0):
+        L = self.L = lib.lib
+        L.gb300_server_create.argtypes = [ctypes.POINTER(ServerConfig)]
+        L.gb300_server_create.restype = ctypes.c_void_p
+        L.gb300_server_destroy.argtypes = [ctypes.c_void_p]
+        L.gb300_server_submit_sigs.argtypes = [ctypes.c_void_p, ctypes.POINTER(SigJob)]
+        L.gb300_server_submit_sigs.restype = ctypes.c_uint64
+        L.gb300_server_submit_poh.argtypes = [ctypes.c_void_p, _u8p, _u64p, ctypes.c_size_t]
+        L.gb300_server_submit_poh.restype = ctypes.c_uint64
+        L.gb300_server_poll.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
+        L.gb300_server_wait.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int]
+        L.gb300_server_release.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
+        L.gb300_server_stats.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]
+        L.gb300_server_times.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(ctypes.c_int64),
+                                         ctypes.POINTER(ctypes.c_int64)]
+        cfg = ServerConfig(device_memory_cap, sig_slots, poh_slots, max_items_per_launch)
+        self.h = L.gb300_server_create(ctypes.byref(cfg))
+        if not self.h:
+            raise RuntimeError("gb300_server_create failed")
+        self._keep = {}
+
+    def submit_sigs(self, sp: SigPackets, kind: int, out: np.ndarray | None = None):
+        """Queues one verify/sign job; returns (ticket, out).  `out` is filled
+        when the ticket completes."""
+        pk = np.ascontiguousarray(sp.concatenated(), dtype=np.uint8)
+        arrs = [np.ascontiguousarray(a, dtype=np.uint32) for a in
+                (sp.message_lens, sp.public_key_offsets, sp.signature_offsets, sp.message_start_offsets)]
+        n = len(arrs[0])
+        if out is None:
+            out = np.zeros(n if kind == JOB_VERIFY else (n, 64), dtype=np.uint8)
+        j = SigJob(_p(pk, _u8p), pk.nbytes, *[_p(a, _u32p) for a in arrs], n, kind, _p(out, _u8p))
+        t = self.L.gb300_server_submit_sigs(self.h, ctypes.byref(j))
+        if t:
+            self._keep[t] = (pk, arrs, out, j)
+        return t, out
+
+    def submit_poh(self, hashes: np.ndarray, num_hashes):
+        nh = np.ascontiguousarray(num_hashes, dtype=np.uint64)
+        assert hashes.dtype == np.uint8 and hashes.flags["C_CONTIGUOUS"]
+        t = self.L.gb300_server_submit_poh(self.h, _p(hashes, _u8p), _p(nh, _u64p), len(nh))
+        if t:
+            self._keep[t] = (hashes, nh)
+        return t
+
+    def poll(self, ticket: int) -> int:
+        return int(self.L.gb300_server_poll(self.h, ticket))
+
+    def wait(self, ticket: int, timeout_ms: int = -1, release: bool = True) -> int:
+        rc = int(self.L.gb300_server_wait(self.h, ticket, timeout_ms))
+        if rc != 0 and release:
+            self.release(ticket)
+        return rc
+
+    def release(self, ticket: int) -> None:
+        self.L.gb300_server_release(self.h, ticket)
+        self._keep.pop(ticket, None)
+
+    def latency_s(self, ticket: int):
+        """Completion minus submission time (seconds), None while pending."""
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        rc = self.L.gb300_server_times(self.h, ticket, ctypes.byref(a), ctypes.byref(b))
+        return (b.value - a.value) * 1e-9 if rc == 1 else None
+
+    def times_ns(self, ticket: int):
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        self.L.gb300_server_times(self.h, ticket, ctypes.byref(a), ctypes.byref(b))
+        return a.value, b.value
+
+    def stats(self) -> dict:
+        import json
+        buf = ctypes.create_string_buffer(1024)
+        n = self.L.gb300_server_stats(self.h, buf, 1024)
+        return json.loads(buf.value[:n].decode()) if n else {}
+
+    def close(self) -> None:
+        if self.h:
+            self.L.gb300_server_destroy(self.h)
+            self.h = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def _buf(b) -> ctypes.Array:
     b = bytes(b)
     return (ctypes.c_uint8 * max(1, len(b))).from_buffer_copy(b if b else b"\0")
