@@ -391,9 +391,9 @@ cudaError_t run_sig_batch(Lease& L, cudaStream_t s, bool sign, const gpu_Elems* 
     const size_t stage_pk_off = round_up(idx_bytes, 256);
     const size_t stage_bytes = stage_pk_off + (all_locked ? 0 : total_bytes);
 
-    TRY(Q.d_data.ensure(total_bytes + 16));
-    TRY(Q.d_index.ensure(idx_bytes));
-    TRY(Q.d_out.ensure(out_bytes));
+    TRY(Q.d_data.ensure(total_bytes + 16, s));
+    TRY(Q.d_index.ensure(idx_bytes, s));
+    TRY(Q.d_out.ensure(out_bytes, s));
     TRY(Q.h_stage.ensure(stage_bytes));
     TRY(Q.h_out.ensure(out_bytes));
 
@@ -534,7 +534,7 @@ int poh_verify_many(uint8_t* hashes, const uint64_t* num_hashes_arr, size_t num_
     cudaStream_t s = use_non_default_stream ? Q.stream : 0;
     const size_t hb = 32ull * num_elems, cb = 8ull * num_elems;
     auto run = [&]() -> cudaError_t {
-        TRY(Q.d_data.ensure(hb + cb));
+        TRY(Q.d_data.ensure(hb + cb, s));
         TRY(Q.h_stage.ensure(hb + cb));
         uint8_t* st = static_cast<uint8_t*>(Q.h_stage.p);
         memcpy(st, hashes, hb);
@@ -606,7 +606,7 @@ int gb300_ed25519_create_keypairs(const uint8_t* seeds, uint8_t* public_keys, ui
     cudaStream_t s = Q.stream;
     auto run = [&]() -> cudaError_t {
         const size_t sb = 32ull * num, pb = 32ull * num, kb = 64ull * num;
-        TRY(Q.d_data.ensure(sb + pb + kb));
+        TRY(Q.d_data.ensure(sb + pb + kb, s));
         TRY(Q.h_stage.ensure(sb + pb + kb));
         uint8_t* st = static_cast<uint8_t*>(Q.h_stage.p);
         uint8_t* d = static_cast<uint8_t*>(Q.d_data.p);
@@ -662,7 +662,7 @@ int ed25519_check_packed_ge_small_order(const unsigned char* packed_group_elemen
     cudaStream_t s = Q.stream;
     uint8_t result = 1;
     auto run = [&]() -> cudaError_t {
-        TRY(Q.d_data.ensure(64));
+        TRY(Q.d_data.ensure(64, s));
         TRY(Q.h_stage.ensure(64));
         uint8_t* st = static_cast<uint8_t*>(Q.h_stage.p);
         uint8_t* d = static_cast<uint8_t*>(Q.d_data.p);
@@ -767,8 +767,8 @@ int gb300_poh_verify_batch(uint8_t* hashes, const uint64_t* num_hashes_arr, size
     const size_t hb = 32ull * num_elems, cb = 8ull * num_elems, wb = poh_batch_workspace_size(num_elems);
     const int warps = 4 * L.dev->sms * T.poh_warps_per_smsp;
     auto run = [&]() -> cudaError_t {
-        TRY(Q.d_data.ensure(hb + cb));
-        TRY(Q.d_scratch.ensure(wb));
+        TRY(Q.d_data.ensure(hb + cb, s));
+        TRY(Q.d_scratch.ensure(wb, s));
         TRY(Q.h_stage.ensure(hb + cb));
         uint8_t* st = static_cast<uint8_t*>(Q.h_stage.p);
         memcpy(st, hashes, hb);
@@ -845,10 +845,10 @@ int gb300_ed25519_batch(const gb300_sig_job* jobs, uint32_t num_jobs) {
         const size_t sig_out_off = round_up(nv, 64);
         const size_t idx_bytes = 16ull * (nv + ns), out_bytes = sig_out_off + 64ull * ns;
         const size_t pk_off = round_up(idx_bytes, 256);
-        TRY(Q.d_data.ensure(total + 16));
-        TRY(Q.d_index.ensure(idx_bytes));
-        TRY(Q.d_out.ensure(out_bytes));
-        TRY(Q.d_scratch.ensure(256));
+        TRY(Q.d_data.ensure(total + 16, s));
+        TRY(Q.d_index.ensure(idx_bytes, s));
+        TRY(Q.d_out.ensure(out_bytes, s));
+        TRY(Q.d_scratch.ensure(256, s));
         TRY(Q.h_stage.ensure(pk_off + (all_locked ? 0 : total)));
         TRY(Q.h_out.ensure(out_bytes));
         uint32_t* hv = static_cast<uint32_t*>(Q.h_stage.p);

@@ -12,8 +12,10 @@
 //     PoH batches on low-priority streams (persistent PoH kernel);
 //   * sleep on a condition variable when there is nothing to do (woken by
 //     submissions; polls the GPU every 20 us while work is in flight).
-// Slot buffers (device rings and page-locked staging) are grow-only and stay
-// resident, as do the basepoint tables.
+// Slot buffers (device rings and page-locked staging) are sized at creation
+// and stay resident, as do the basepoint tables; merged launches are kept
+// within a slot's ring, so steady-state serving never allocates (a single
+// request larger than a ring grows it with the stream-ordered allocator).
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -116,10 +118,10 @@ cudaError_t launch_sigs(gb300_server* sv, Slot& S) {
     const size_t idx_bytes = 16ull * (nv + ns), out_bytes = S.sig_out_off + 64ull * ns;
     const size_t pk_off = round_up(idx_bytes, 256);
     cudaError_t e;
-    if ((e = S.d_data.ensure(total + 16)) != cudaSuccess) return e;
-    if ((e = S.d_index.ensure(idx_bytes)) != cudaSuccess) return e;
-    if ((e = S.d_out.ensure(out_bytes)) != cudaSuccess) return e;
-    if ((e = S.d_scratch.ensure(256)) != cudaSuccess) return e;
+    if ((e = S.d_data.ensure(total + 16, S.stream)) != cudaSuccess) return e;
+    if ((e = S.d_index.ensure(idx_bytes, S.stream)) != cudaSuccess) return e;
+    if ((e = S.d_out.ensure(out_bytes, S.stream)) != cudaSuccess) return e;
+    if ((e = S.d_scratch.ensure(256, S.stream)) != cudaSuccess) return e;
     if ((e = S.h_stage.ensure(pk_off + (locked ? 0 : total))) != cudaSuccess) return e;
     if ((e = S.h_out.ensure(out_bytes)) != cudaSuccess) return e;
     uint32_t* hv = static_cast<uint32_t*>(S.h_stage.p);
@@ -179,8 +181,8 @@ cudaError_t launch_pohs(gb300_server* sv, Slot& S) {
     S.poh_n = n;
     const size_t hb = 32ull * n, cb = 8ull * n;
     cudaError_t e;
-    if ((e = S.d_data.ensure(hb + cb)) != cudaSuccess) return e;
-    if ((e = S.d_scratch.ensure(poh_batch_workspace_size(n))) != cudaSuccess) return e;
+    if ((e = S.d_data.ensure(hb + cb, S.stream)) != cudaSuccess) return e;
+    if ((e = S.d_scratch.ensure(poh_batch_workspace_size(n), S.stream)) != cudaSuccess) return e;
     if ((e = S.h_stage.ensure(hb + cb)) != cudaSuccess) return e;
     uint8_t* st = static_cast<uint8_t*>(S.h_stage.p);
     uint64_t pos = 0;
@@ -265,13 +267,18 @@ void dispatcher(gb300_server* sv) {
         bool launched = false;
         for (auto& S : sv->sig_slots) {
             if (S.busy || sv->pending_sig.empty()) continue;
-            uint64_t items = 0, bytes = 0;
+            uint64_t items = 0, bytes = 0, pkt = 0;
             while (!sv->pending_sig.empty()) {
                 const Req& r = sv->pending_sig.front();
-                if (!S.reqs.empty() && (items + r.n > sv->max_items || sv->in_use + bytes + r.bytes > sv->cap)) break;
+                // merge while the launch fits the item cap, the memory budget
+                // and the slot's resident packet ring (no reallocation)
+                if (!S.reqs.empty() && (items + r.n > sv->max_items || sv->in_use + bytes + r.bytes > sv->cap ||
+                                        pkt + r.job.packets_len + 16 > S.d_data.cap))
+                    break;
                 if (S.reqs.empty() && sv->in_use + r.bytes > sv->cap) break;   // wait for memory
                 items += r.n;
                 bytes += r.bytes;
+                pkt += r.job.packets_len;
                 S.reqs.push_back(r);
                 sv->pending_sig.pop_front();
             }
@@ -348,6 +355,24 @@ gb300_server* gb300_server_create(const gb300_server_config* cfg) {
     for (auto& S : sv->poh_slots)
         ok = ok && cudaStreamCreateWithPriority(&S.stream, cudaStreamNonBlocking, lo) == cudaSuccess &&
              cudaEventCreateWithFlags(&S.done, cudaEventDisableTiming) == cudaSuccess;
+    // resident rings: each signature slot holds a 64 MiB packet ring and the
+    // index/output space of a full launch; each PoH slot 65536 entries
+    for (auto& S : sv->sig_slots) {
+        const uint64_t mi = sv->max_items;
+        ok = ok && S.d_data.ensure(64ull << 20, S.stream) == cudaSuccess &&
+             S.d_index.ensure(16 * mi, S.stream) == cudaSuccess &&
+             S.d_out.ensure(round_up(mi, 64) + 64 * mi, S.stream) == cudaSuccess &&
+             S.d_scratch.ensure(256, S.stream) == cudaSuccess &&
+             S.h_stage.ensure(round_up(16 * mi, 256) + (64ull << 20)) == cudaSuccess &&
+             S.h_out.ensure(round_up(mi, 64) + 64 * mi) == cudaSuccess;
+    }
+    for (auto& S : sv->poh_slots) {
+        ok = ok && S.d_data.ensure(40ull * 65536, S.stream) == cudaSuccess &&
+             S.d_scratch.ensure(poh_batch_workspace_size(65536), S.stream) == cudaSuccess &&
+             S.h_stage.ensure(40ull * 65536) == cudaSuccess;
+    }
+    for (auto* slots : {&sv->sig_slots, &sv->poh_slots})
+        for (auto& S : *slots) ok = ok && cudaStreamSynchronize(S.stream) == cudaSuccess;
     if (!ok) {
         gb300_server_destroy(sv);
         return nullptr;
