@@ -63,6 +63,11 @@ void gb300_server_release(gb300_server* s, uint64_t ticket);
  * is -1 while pending); returns 1 when complete, 0 while pending. */
 int gb300_server_times(gb300_server* s, uint64_t ticket, int64_t* submit_ns, int64_t* done_ns);
 
+/* Timeline of the most recent launches as a JSON array of
+ * [kind (0 signatures, 2 PoH), requests merged, items, admitted_ns,
+ *  enqueued_ns, completed_ns]; returns the length written. */
+int gb300_server_trace(gb300_server* s, char* buf, size_t len);
+
 /* Counters as a JSON object; returns the length written. */
 int gb300_server_stats(gb300_server* s, char* buf, size_t len);
 

@@ -60,6 +60,7 @@ struct Req {
 };
 
 struct Slot {
+    int64_t t_admit = 0, t_enqueued = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     bool busy = false;
@@ -90,6 +91,15 @@ struct gb300_server {
     std::thread worker;
     // counters
     uint64_t launches_sig = 0, launches_poh = 0, requests_done = 0, merged_max = 0, items_done = 0;
+    // per-launch timeline of the last launches: kind, requests, items,
+    // admitted / enqueued / observed complete (steady ns)
+    struct Trace {
+        int kind;
+        uint32_t reqs;
+        uint64_t items;
+        int64_t t_admit, t_enqueued, t_complete;
+    };
+    std::vector<Trace> trace;
 };
 
 namespace {
@@ -249,6 +259,12 @@ void dispatcher(gb300_server* sv) {
                 deliver(S);
                 lk.lock();
                 const int64_t t_done = now_ns();
+                {
+                    uint64_t it = 0;
+                    for (auto& r : S.reqs) it += r.n;
+                    if (sv->trace.size() >= 4096) sv->trace.erase(sv->trace.begin(), sv->trace.begin() + 1024);
+                    sv->trace.push_back({S.kind, (uint32_t)S.reqs.size(), it, S.t_admit, S.t_enqueued, t_done});
+                }
                 for (auto& r : S.reqs) {
                     sv->times[r.ticket].second = t_done;
                     sv->status[r.ticket] = S.err == cudaSuccess ? 1 : -(int)S.err;
@@ -289,8 +305,10 @@ void dispatcher(gb300_server* sv) {
             sv->in_use += bytes;
             sv->launches_sig++;
             if (S.reqs.size() > sv->merged_max) sv->merged_max = S.reqs.size();
+            S.t_admit = now_ns();
             lk.unlock();
             S.err = launch_sigs(sv, S);
+            S.t_enqueued = now_ns();
             lk.lock();
             launched = true;
         }
@@ -310,8 +328,10 @@ void dispatcher(gb300_server* sv) {
             S.bytes = bytes;
             sv->in_use += bytes;
             sv->launches_poh++;
+            S.t_admit = now_ns();
             lk.unlock();
             S.err = launch_pohs(sv, S);
+            S.t_enqueued = now_ns();
             lk.lock();
             launched = true;
         }
@@ -486,6 +506,28 @@ int gb300_server_times(gb300_server* sv, uint64_t ticket, int64_t* submit_ns, in
     if (submit_ns) *submit_ns = it->second.first;
     if (done_ns) *done_ns = it->second.second;
     return it->second.second >= 0 ? 1 : 0;
+}
+
+int gb300_server_trace(gb300_server* sv, char* buf, size_t len) {
+    if (!sv || !buf || len == 0) return 0;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    size_t off = 0;
+    int n = snprintf(buf, len, "[");
+    if (n < 0) return 0;
+    off = (size_t)n;
+    for (size_t i = 0; i < sv->trace.size() && off + 128 < len; i++) {
+        const auto& t = sv->trace[i];
+        n = snprintf(buf + off, len - off, "%s[%d,%u,%llu,%lld,%lld,%lld]", i ? "," : "", t.kind, t.reqs,
+                     (unsigned long long)t.items, (long long)t.t_admit, (long long)t.t_enqueued,
+                     (long long)t.t_complete);
+        if (n < 0) break;
+        off += (size_t)n;
+    }
+    if (off + 2 <= len) {
+        buf[off++] = ']';
+        buf[off] = 0;
+    }
+    return (int)off;
 }
 
 int gb300_server_stats(gb300_server* sv, char* buf, size_t len) {
