@@ -39,6 +39,11 @@ for _p in (REPO, PKG):
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
+# streams beyond the hardware work-queue count share queues (false
+# dependencies between, e.g., a verify launch and a PoH kernel): ask for the
+# maximum before torch creates the CUDA context
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 # one GPU per rank: the C ABI's pool spreads calls over every visible GPU,
 # so each rank sees only its own
 if "LOCAL_RANK" in os.environ and "CUDA_VISIBLE_DEVICES" not in os.environ:

@@ -106,8 +106,18 @@ int g_num_gpus = -1;  // -1: not initialised yet
 Device g_dev[kMaxGpus];
 uint32_t g_next_gpu = 0;
 
+// Streams beyond CUDA_DEVICE_MAX_CONNECTIONS (default 8) share hardware work
+// queues, so a short verify launch can end up queued behind a second-long
+// PoH kernel on an unrelated stream.  Ask for the maximum before the CUDA
+// context exists (it has no effect once the process has created it; a host
+// application that creates it first should set the variable itself).
+void request_connections() {
+    if (!getenv("CUDA_DEVICE_MAX_CONNECTIONS")) setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0);
+}
+
 bool init_locked() {
     if (g_num_gpus >= 0) return g_num_gpus > 0;
+    request_connections();
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess) {
         cudaGetLastError();
@@ -121,9 +131,8 @@ bool init_locked() {
         if (cudaSetDevice(d) != cudaSuccess) break;
         Device& D = g_dev[d];
         D.id = d;
-        bool ok = true;
-        for (int k = 0; k < kQueues && ok; k++)
-            ok = cudaStreamCreateWithFlags(&D.q[k].stream, cudaStreamNonBlocking) == cudaSuccess;
+        // queue 0's stream now (tables); the others on first use
+        bool ok = cudaStreamCreateWithFlags(&D.q[0].stream, cudaStreamNonBlocking) == cudaSuccess;
         if (ok) ok = crypt_tables_create(&D.tables, D.q[0].stream) == cudaSuccess;
         if (ok) ok = cudaDeviceGetAttribute(&D.sms, cudaDevAttrMultiProcessorCount, d) == cudaSuccess;
         if (!ok) {
@@ -160,6 +169,12 @@ bool acquire(Lease& L) {
     L.dev = &D;
     L.q = &Q;
     cudaSetDevice(D.id);
+    if (!Q.stream && cudaStreamCreateWithFlags(&Q.stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        Q.mu.unlock();
+        L.q = nullptr;
+        return false;
+    }
     return true;
 }
 

@@ -21,6 +21,7 @@
 #include <chrono>
 #include <condition_variable>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <mutex>
@@ -352,6 +353,9 @@ void dispatcher(gb300_server* sv) {
 extern "C" {
 
 gb300_server* gb300_server_create(const gb300_server_config* cfg) {
+    // more streams than hardware work queues would make signature launches
+    // wait behind PoH kernels (see crypt_api.cu request_connections)
+    if (!getenv("CUDA_DEVICE_MAX_CONNECTIONS")) setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0);
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
     auto* sv = new gb300_server();

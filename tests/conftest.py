@@ -11,6 +11,11 @@ for p in (REPO, PKG):
     if p not in sys.path:
         sys.path.insert(0, p)
 
+# as the library does when it creates the CUDA context itself: enough hardware
+# work queues that unrelated streams do not serialise (torch may create the
+# context first)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs the CUDA library)")
