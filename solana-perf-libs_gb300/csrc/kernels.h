@@ -46,7 +46,7 @@ cudaError_t launch_poh_verify(uint8_t* hashes, const uint64_t* num_hashes, uint6
 // `workspace` holds poh_batch_workspace_size(n) bytes of device memory.
 size_t poh_batch_workspace_size(uint64_t n);
 cudaError_t launch_poh_batch(uint8_t* hashes, const uint64_t* counts, uint64_t n, void* workspace, int warps,
-                             cudaStream_t s);
+                             cudaStream_t s, int block_warps = 1);
 
 // Mixed verify + sign work for one persistent launch (sig_batch.cu).  Both
 // batches index the same packet buffer.  Verify items are chunks

@@ -73,7 +73,7 @@ __device__ __forceinline__ void store_entry(uint8_t* hashes, uint32_t e, const u
     p[1] = make_uint4(bswap_u32(w[4]), bswap_u32(w[5]), bswap_u32(w[6]), bswap_u32(w[7]));
 }
 
-__global__ void __launch_bounds__(32) poh_persistent_kernel(uint8_t* hashes, const uint64_t* counts, uint32_t n,
+__global__ void __launch_bounds__(128) poh_persistent_kernel(uint8_t* hashes, const uint64_t* counts, uint32_t n,
                                                             PohBatchScratch* s, uint32_t one) {
     const uint32_t lane = threadIdx.x & 31u;
     const PohMul M(one);
@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(32) poh_persistent_kernel(uint8_t* hashes, con
 size_t poh_batch_workspace_size(uint64_t n) { return sizeof(PohBatchScratch) + 4ull * (n ? n : 1); }
 
 cudaError_t launch_poh_batch(uint8_t* hashes, const uint64_t* counts, uint64_t n, void* workspace,
-                             int warps, cudaStream_t s) {
+                             int warps, cudaStream_t s, int block_warps) {
     if (n == 0) return cudaSuccess;
     if (n > 0xffffffffull) return cudaErrorInvalidValue;
     PohBatchScratch* sc = static_cast<PohBatchScratch*>(workspace);
@@ -137,9 +137,14 @@ cudaError_t launch_poh_batch(uint8_t* hashes, const uint64_t* counts, uint64_t n
     poh_hist_kernel<<<blocks, 256, 0, s>>>(counts, n, sc);
     poh_scan_kernel<<<1, 32, 0, s>>>(sc);
     poh_scatter_kernel<<<blocks, 256, 0, s>>>(counts, n, sc);
+    // every warp is independent; block_warps only decides how warps are
+    // packed onto SMs (1: spread over as many SMs as possible; 4: one warp per
+    // sub-partition on as few SMs as possible, leaving the rest to other work)
+    if (block_warps < 1 || block_warps > 4) block_warps = 1;
     uint64_t need = (n + 31) / 32;
-    unsigned grid = (unsigned)(need < (uint64_t)warps ? need : (uint64_t)warps);
-    poh_persistent_kernel<<<grid, 32, 0, s>>>(hashes, counts, (uint32_t)n, sc, 1u);
+    uint64_t nwarps = need < (uint64_t)warps ? need : (uint64_t)warps;
+    unsigned grid = (unsigned)((nwarps + block_warps - 1) / block_warps);
+    poh_persistent_kernel<<<grid, 32 * block_warps, 0, s>>>(hashes, counts, (uint32_t)n, sc, 1u);
     return cudaGetLastError();
 }
 
