@@ -46,8 +46,20 @@ os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 # one GPU per rank: the C ABI's pool spreads calls over every visible GPU,
 # so each rank sees only its own
-if "LOCAL_RANK" in os.environ and "CUDA_VISIBLE_DEVICES" not in os.environ:
-    os.environ["CUDA_VISIBLE_DEVICES"] = os.environ["LOCAL_RANK"]
+def _pin_rank_gpu():
+    lr = os.environ.get("LOCAL_RANK")
+    if lr is None:
+        return
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if vis is None:
+        os.environ["CUDA_VISIBLE_DEVICES"] = lr
+    elif vis.strip():
+        ids = [v.strip() for v in vis.split(",") if v.strip()]
+        if int(lr) < len(ids):
+            os.environ["CUDA_VISIBLE_DEVICES"] = ids[int(lr)]
+
+
+_pin_rank_gpu()
 
 import numpy as np  # noqa: E402
 
