@@ -274,6 +274,36 @@ def bench_verify_device(lib, torch, sp, steps, warmup):
     return sum(a.elapsed_time(b) for a, b in evs) * 1e-3, out.cpu().numpy()
 
 
+def bench_sign_device(lib, torch, n, reps=3):
+    """Signing throughput on a GPU-filling batch, inputs resident on the GPU:
+    packets [64-B private key][32-B public key][64-B message]."""
+    rng = np.random.default_rng(11)
+    seeds = rng.integers(0, 256, (n, 32), dtype=np.uint8)
+    pk, sk = lib.create_keypairs(seeds)
+    stride = 160
+    pkt = np.zeros((n, stride), dtype=np.uint8)
+    pkt[:, 0:64] = sk
+    pkt[:, 64:96] = pk
+    pkt[:, 96:] = rng.integers(0, 256, (n, 64), dtype=np.uint8)
+    idx = np.arange(n, dtype=np.int64) * stride
+    stream = torch.cuda.current_stream()
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    d_pk = dev(pkt.ravel())
+    arrs = [dev(np.full(n, 64, dtype=np.int32)), dev((idx + 64).astype(np.int32)), dev(idx.astype(np.int32)),
+            dev((idx + 96).astype(np.int32))]
+    out = torch.zeros((n, 64), dtype=torch.uint8, device="cuda")
+    best = 1e30
+    for it in range(reps + 1):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        lib.sign_device(d_pk, *arrs, out, stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if it:
+            best = min(best, e0.elapsed_time(e1) * 1e-3)
+    return n / best, best
+
+
 def bench_verify_e2e(lib, sp, steps, warmup):
     for _ in range(warmup):
         lib.verify_many(sp)
@@ -582,6 +612,23 @@ def cpu_poh(h0, cnt, nthreads, sample_entries):
     return float(c.sum()) / dt
 
 
+def cpu_sign(nthreads, n=8192):
+    from oracle.oracle import get_oracle
+    import workloads
+    o = get_oracle()
+    sp, _ = workloads.verify_uniform(o.create_keypairs, o.sign_packets, n=64, seed=12)   # warm tables
+    rng = np.random.default_rng(12)
+    pk, sk = o.create_keypairs(rng.integers(0, 256, (n, 32), dtype=np.uint8))
+    stride = 160
+    pkt = np.zeros((n, stride), dtype=np.uint8)
+    pkt[:, 0:64], pkt[:, 64:96] = sk, pk
+    pkt[:, 96:] = rng.integers(0, 256, (n, 64), dtype=np.uint8)
+    idx = np.arange(n, dtype=np.uint32) * stride
+    t = time.perf_counter()
+    o.sign_many(pkt.ravel(), np.full(n, 64, dtype=np.uint32), idx + 64, idx, idx + 96, nthreads)
+    return n / (time.perf_counter() - t)
+
+
 def cpu_verify(sp, nthreads, reps):
     from oracle.oracle import get_oracle
     o = get_oracle()
@@ -663,6 +710,16 @@ def run_ours(args):
                      "peak_source": "measured mad.wide.u32 throughput (gb300_int_peak_launch), 'of measured'"},
         "gpu_launches": vsteps,
     }
+    sign_value, sign_s = bench_sign_device(lib, torch, VERIFY_BIG_N)
+    sign = {"metric": "Ed25519 signs/s", "unit": "signs/s", "value": sign_value,
+            "config": {"workload": f"{VERIFY_BIG_N} packets [64-B private key][32-B public key][64-B message], "
+                                   "device-resident", "signatures": VERIFY_BIG_N},
+            "ms_per_launch": sign_s * 1e3,
+            "roofline": {"bound": "int_imad_wide", "achieved": sign_value * SIGN_MACS / 1e12,
+                         "peak": peaks["mad_wide"] / 1e12, "unit": "Tmac/s",
+                         "frac": sign_value * SIGN_MACS / peaks["mad_wide"], "macs_per_unit": SIGN_MACS,
+                         "traffic": traffic.get("ed25519_sign_kernel"),
+                         "peak_source": "measured mad.wide.u32 throughput (gb300_int_peak_launch), 'of measured'"}}
     # ---- CPU baselines (rank 0, N = 1) ----
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         sample = POH_ENTRIES
@@ -674,7 +731,10 @@ def run_ours(args):
         verify["cpu_baseline"] = {"value": cpu_verify(sp, nthreads, reps), "unit": "verifies/s",
                                   "cores": nthreads, "kind": "port",
                                   "sample": f"{reps} x 1024 verifies on {nthreads} threads, CPU oracle"}
+        sign["cpu_baseline"] = {"value": cpu_sign(nthreads), "unit": "signs/s", "cores": nthreads, "kind": "port",
+                                "sample": f"8192 signs of 64-B messages on {nthreads} threads, CPU oracle"}
     line["ed25519_verify"] = verify
+    line["ed25519_sign"] = sign
     if not args.skip_ragged:
         line["poh_ragged"] = bench_poh_ragged(lib, torch, steps=2)
         line["ragged_sigs"] = bench_ragged_sigs(lib, torch)
