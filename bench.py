@@ -671,10 +671,13 @@ def run_ours(args):
                    "l2": "flushed between steps (256 MB write)", "stream": "torch current stream"},
         "roofline": {"bound": "int_alu", "achieved": achieved_ops / 1e12, "peak": peaks["lop3"] / 1e12,
                      "unit": "Tops/s", "frac": achieved_ops / peaks["lop3"],
-                     "traffic": traffic.get("poh_verify_kernel"),
+                     "traffic": traffic.get("poh_pair_kernel"),
+                     "kernel": "poh_pair_kernel (two warps per 32 chains)",
                      "ops_per_unit": POH_OPS_PER_HASH,
                      "peak_source": "measured lop3.b32 throughput (gb300_int_peak_launch), 'of measured'",
-                     "parallelism_cap": "4096 chains = 128 warps on 608 SM sub-partitions"},
+                     "parallelism_cap": "4096 chains = 128 round warps + 128 schedule warps on 608 SM "
+                                        "sub-partitions; a chain is serial, so each round warp is bound by "
+                                        "its own sub-partition's ALU issue rate"},
         "e2e": {"value": e2e_value, "unit": "hashes/s", "h2d_bytes_per_step": POH_ENTRIES * 40,
                 "d2h_bytes_per_step": POH_ENTRIES * 32, "path": "poh_verify_many (C ABI, host buffers)"},
         "gpu_launches": args.steps,
