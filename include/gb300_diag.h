@@ -1,7 +1,8 @@
 /*
  * gb300_diag.h -- diagnostics of libcuda-crypt.so (no counterpart in the
  * reference): integer-pipe throughput microbenchmarks used as the
- * denominators of the integer roofline that the benchmark reports.
+ * denominators of the integer roofline that the benchmark reports, and a
+ * PoH batch entry point with a forced launch shape.
  */
 #ifndef GB300_CRYPT_DIAG_H
 #define GB300_CRYPT_DIAG_H
@@ -19,6 +20,15 @@ extern "C" {
  * the kernel may write.  Enqueued on `stream`; returns a cudaError_t. */
 int gb300_int_peak_launch(int kind, uint32_t blocks, uint32_t threads, uint32_t iters, uint32_t* sink,
                           void* stream);
+
+/* gb300_poh_verify_batch_device with the launch shape forced instead of
+ * tuned: `warps` resident warps (1 .. 64 x SM count) of the persistent
+ * kernel, packed `block_warps` per block: 1 (one warp per 32 chains),
+ * 2 (paired schedule and round warps per 32 chains) or 4 (four single warps
+ * per block).  Same results as every other PoH entry point; used to test
+ * and time each form.  Returns a cudaError_t. */
+int gb300_poh_verify_batch_shape(uint8_t* hashes, const uint64_t* num_hashes, uint64_t num_elems, void* workspace,
+                                 size_t workspace_bytes, int warps, int block_warps, void* stream);
 
 #ifdef __cplusplus
 }

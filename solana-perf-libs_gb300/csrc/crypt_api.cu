@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <atomic>
 #include <cstdio>
 #include <cstdlib>
@@ -86,8 +87,9 @@ struct Tuning {
     int sig_threads = 128;        // threads per block of the persistent sign/verify kernel
     int sig_blocks_per_sm = 0;    // 0 = as many as fit
     int poh_warps_per_smsp = 1;   // resident warps of the persistent PoH kernel per SM sub-partition
+    int poh_block_warps = 1;      // 1: one warp per 32 lanes; 2: paired schedule + round warps
     double sig_ms[3] = {0, 0, 0}; // calibration times for 64 / 128 / 256 threads
-    double poh_ms[2] = {0, 0};    // calibration times for 1 / 2 warps per sub-partition
+    double poh_ms[3] = {0, 0, 0}; // calibration: single 1 and 2 warps per sub-partition, paired
     int calib_sigs = 0, calib_chains = 0;
 };
 
@@ -337,12 +339,18 @@ void tune_device(Device& D) {
         T.calib_sigs = (int)(nv + ns);
     }
     cudaFree(dseed); cudaFree(dpk); cudaFree(dsk); cudaFree(dsig); cudaFree(dpkt); cudaFree(dout); cudaFree(didx);
-    // ---- PoH ----
-    const uint32_t nc = (uint32_t)sms * 4u * 32u * 2u;
+    // ---- PoH: ragged chains, counts log-uniform in 1..20000 (the longest
+    // chain bounds the launch, as in real ragged batches) ----
+    const uint32_t nc = 16384;
     std::vector<uint8_t> hh(32ull * nc);
     std::vector<uint64_t> hc(nc);
     for (auto& b : hh) b = (uint8_t)splitmix(rs);
-    for (auto& c : hc) c = 1 + splitmix(rs) % 2000u;
+    for (auto& c : hc) {
+        const double u = (double)(splitmix(rs) >> 11) * (1.0 / 9007199254740992.0);
+        c = (uint64_t)exp(u * log(20001.0));
+        if (c < 1) c = 1;
+        if (c > 20000) c = 20000;
+    }
     uint8_t* dh = nullptr;
     uint64_t* dc = nullptr;
     void* ws = nullptr;
@@ -351,13 +359,18 @@ void tune_device(Device& D) {
         cudaMemcpyAsync(dh, hh.data(), hh.size(), cudaMemcpyHostToDevice, s);
         cudaMemcpyAsync(dc, hc.data(), 8ull * nc, cudaMemcpyHostToDevice, s);
         double best = 1e30;
-        for (int wps = 1; wps <= 2; wps++) {
+        const int mode_wps[3] = {1, 2, 1}, mode_bw[3] = {1, 1, 2};
+        for (int m = 0; m < 3; m++) {
             cudaError_t err = cudaSuccess;
-            float ms = time_ms(s, [&]() { return launch_poh_batch(dh, dc, nc, ws, 4 * sms * wps, s); }, err);
-            T.poh_ms[wps - 1] = ms;
+            launch_poh_batch(dh, dc, nc, ws, 4 * sms * mode_wps[m], s, mode_bw[m]);   // warm
+            cudaStreamSynchronize(s);
+            float ms = time_ms(
+                s, [&]() { return launch_poh_batch(dh, dc, nc, ws, 4 * sms * mode_wps[m], s, mode_bw[m]); }, err);
+            T.poh_ms[m] = ms;
             if (err == cudaSuccess && ms < best) {
                 best = ms;
-                T.poh_warps_per_smsp = wps;
+                T.poh_warps_per_smsp = mode_wps[m];
+                T.poh_block_warps = mode_bw[m];
             }
         }
         T.calib_chains = (int)nc;
@@ -368,6 +381,7 @@ void tune_device(Device& D) {
     T.sig_threads = env_int("GB300_CRYPT_SIG_THREADS", T.sig_threads);
     T.sig_blocks_per_sm = env_int("GB300_CRYPT_SIG_BLOCKS", T.sig_blocks_per_sm);
     T.poh_warps_per_smsp = env_int("GB300_CRYPT_POH_WARPS_PER_SMSP", T.poh_warps_per_smsp);
+    T.poh_block_warps = env_int("GB300_CRYPT_POH_PAIRED", T.poh_block_warps == 2) ? 2 : 1;
     LOG("tuned gpu %d: sig threads %d (ms %.3f %.3f %.3f), poh warps/smsp %d (ms %.3f %.3f)\n", D.id, T.sig_threads,
         T.sig_ms[0], T.sig_ms[1], T.sig_ms[2], T.poh_warps_per_smsp, T.poh_ms[0], T.poh_ms[1]);
 }
@@ -747,28 +761,48 @@ int gb300_crypt_tuning(char* buf, size_t len) {
     int n = snprintf(buf, len,
                      "{\"device\": %d, \"sms\": %d, \"sig_threads\": %d, \"sig_blocks_per_sm\": %d, "
                      "\"sig_calibration_ms\": {\"64\": %.4f, \"128\": %.4f, \"256\": %.4f}, "
-                     "\"sig_calibration_items\": %d, \"poh_warps_per_smsp\": %d, "
-                     "\"poh_calibration_ms\": {\"1\": %.4f, \"2\": %.4f}, \"poh_calibration_chains\": %d}",
+                     "\"sig_calibration_items\": %d, \"poh_warps_per_smsp\": %d, \"poh_paired\": %d, "
+                     "\"poh_calibration_ms\": {\"single_1\": %.4f, \"single_2\": %.4f, \"paired\": %.4f}, "
+                     "\"poh_calibration_chains\": %d}",
                      D->id, D->sms, T.sig_threads, T.sig_blocks_per_sm, T.sig_ms[0], T.sig_ms[1], T.sig_ms[2],
-                     T.calib_sigs, T.poh_warps_per_smsp, T.poh_ms[0], T.poh_ms[1], T.calib_chains);
+                     T.calib_sigs, T.poh_warps_per_smsp, T.poh_block_warps == 2, T.poh_ms[0], T.poh_ms[1],
+                     T.poh_ms[2], T.calib_chains);
     return n < 0 ? 0 : (n < (int)len ? n : (int)len - 1);
 }
 
 size_t gb300_poh_batch_workspace_size(uint64_t num_elems) { return poh_batch_workspace_size(num_elems); }
 
-int gb300_poh_verify_batch_device(uint8_t* hashes, const uint64_t* num_hashes, uint64_t num_elems, void* workspace,
-                                  size_t workspace_bytes, void* stream) {
-    if (num_elems == 0) return 0;
+static int poh_batch_device_checks(const uint8_t* hashes, const uint64_t* num_hashes, uint64_t num_elems,
+                                   const void* workspace, size_t workspace_bytes) {
     if (num_elems > 0xffffffffull) return (int)cudaErrorInvalidValue;
     if ((reinterpret_cast<uintptr_t>(hashes) & 15u) || (reinterpret_cast<uintptr_t>(num_hashes) & 7u) ||
         (reinterpret_cast<uintptr_t>(workspace) & 15u))
         return (int)cudaErrorMisalignedAddress;
     if (workspace_bytes < poh_batch_workspace_size(num_elems)) return (int)cudaErrorInvalidValue;
+    return 0;
+}
+
+int gb300_poh_verify_batch_device(uint8_t* hashes, const uint64_t* num_hashes, uint64_t num_elems, void* workspace,
+                                  size_t workspace_bytes, void* stream) {
+    if (num_elems == 0) return 0;
+    if (int rc = poh_batch_device_checks(hashes, num_hashes, num_elems, workspace, workspace_bytes)) return rc;
     Device* D = current_device();
     if (!D) return (int)cudaErrorNoDevice;
     const Tuning& T = tuning_for(*D);
     return (int)launch_poh_batch(hashes, num_hashes, num_elems, workspace, 4 * D->sms * T.poh_warps_per_smsp,
-                                 static_cast<cudaStream_t>(stream));
+                                 static_cast<cudaStream_t>(stream), T.poh_block_warps);
+}
+
+int gb300_poh_verify_batch_shape(uint8_t* hashes, const uint64_t* num_hashes, uint64_t num_elems, void* workspace,
+                                 size_t workspace_bytes, int warps, int block_warps, void* stream) {
+    if (num_elems == 0) return 0;
+    if (int rc = poh_batch_device_checks(hashes, num_hashes, num_elems, workspace, workspace_bytes)) return rc;
+    if (block_warps != 1 && block_warps != 2 && block_warps != 4) return (int)cudaErrorInvalidValue;
+    Device* D = current_device();
+    if (!D) return (int)cudaErrorNoDevice;
+    if (warps < 1 || warps > 64 * D->sms) return (int)cudaErrorInvalidValue;
+    return (int)launch_poh_batch(hashes, num_hashes, num_elems, workspace, warps, static_cast<cudaStream_t>(stream),
+                                 block_warps);
 }
 
 int gb300_poh_verify_batch(uint8_t* hashes, const uint64_t* num_hashes_arr, size_t num_elems) {
@@ -792,9 +826,9 @@ int gb300_poh_verify_batch(uint8_t* hashes, const uint64_t* num_hashes_arr, size
         const uint64_t* dc = reinterpret_cast<const uint64_t*>(d + hb);
         TRY(cudaMemcpyAsync(d, st, hb + cb, cudaMemcpyHostToDevice, s));
         std::vector<uint64_t> key = {num_elems, (uint64_t)(uintptr_t)d, (uint64_t)(uintptr_t)Q.d_scratch.p,
-                                     (uint64_t)warps};
+                                     (uint64_t)warps, (uint64_t)T.poh_block_warps};
         TRY(run_graph(Q.g_poh, key, s, [&](cudaStream_t cs) {
-            return launch_poh_batch(d, dc, num_elems, Q.d_scratch.p, warps, cs);
+            return launch_poh_batch(d, dc, num_elems, Q.d_scratch.p, warps, cs, T.poh_block_warps);
         }));
         TRY(cudaMemcpyAsync(st, d, hb, cudaMemcpyDeviceToHost, s));
         TRY(cudaStreamSynchronize(s));

@@ -125,6 +125,131 @@ __global__ void __launch_bounds__(32 * BW) poh_persistent_kernel(uint8_t* hashes
     }
 }
 
+// Paired form: two warps per 32 lanes, as in poh.cu's poh_pair_kernel (warp
+// 1 computes the message schedule into shared memory while warp 0 runs the
+// rounds), inside the persistent longest-first loop.  Warp 0 owns the queue:
+// each refill round it stores finished chains, loads new ones and the step
+// count r (the smallest remaining count among its busy lanes), and hands the
+// current hash words and r to warp 1 through shared memory at barrier 5;
+// then both run r hashes with barriers 1-4 per hash.  r == 0 means every
+// lane is done and both warps leave together.
+__device__ __forceinline__ uint32_t sched_s0(uint32_t x) { return POH_ROTR(x, 7) ^ POH_ROTR(x, 18) ^ (x >> 3); }
+__device__ __forceinline__ uint32_t sched_s1(uint32_t x) { return POH_ROTR(x, 17) ^ POH_ROTR(x, 19) ^ (x >> 10); }
+
+__global__ void __launch_bounds__(64) poh_pair_persistent_kernel(uint8_t* hashes, const uint64_t* counts, uint32_t n,
+                                                                 PohBatchScratch* s) {
+    __shared__ uint32_t kw[48][32];
+    __shared__ uint32_t hout[8][32];
+    __shared__ uint64_t run_len;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t iv[8] = {0x6a09e667u, 0xbb67ae85u, 0x3c6ef372u, 0xa54ff53au,
+                            0x510e527fu, 0x9b05688cu, 0x1f83d9abu, 0x5be0cd19u};
+    uint32_t w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    uint64_t rem = 0;
+    uint32_t cur = 0xffffffffu;
+    bool done = false;
+    for (;;) {
+        if (warp == 0) {
+            for (;;) {
+                const bool need = !done && rem == 0;
+                const uint32_t mask = __ballot_sync(0xffffffffu, need);
+                if (mask == 0) break;
+                if (need && cur != 0xffffffffu) {
+                    store_entry(hashes, cur, w);
+                    cur = 0xffffffffu;
+                }
+                uint32_t base = 0;
+                if (lane == (uint32_t)(__ffs(mask) - 1)) base = atomicAdd(&s->next, (uint32_t)__popc(mask));
+                base = __shfl_sync(0xffffffffu, base, __ffs(mask) - 1);
+                if (need) {
+                    const uint32_t k = base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+                    if (k >= n) {
+                        done = true;
+                    } else {
+                        cur = s->order[k];
+                        load_entry(hashes, cur, w);
+                        rem = counts[cur];
+                    }
+                }
+            }
+            uint64_t r = done ? ~0ull : rem;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const uint64_t other = __shfl_xor_sync(0xffffffffu, r, o);
+                r = other < r ? other : r;
+            }
+            if (r == ~0ull) r = 0;
+#pragma unroll
+            for (int t = 0; t < 8; t++) hout[t][lane] = w[t];
+            if (lane == 0) run_len = r;
+        }
+        asm volatile("bar.sync 5, 64;" ::: "memory");
+        const uint64_t r = run_len;
+        if (r == 0) break;
+        if (warp == 1) {
+#pragma unroll
+            for (int t = 0; t < 8; t++) w[t] = hout[t][lane];
+#pragma unroll 1
+            for (uint64_t k = 0; k < r; k++) {
+                uint32_t W[16];
+#pragma unroll
+                for (int t = 0; t < 8; t++) W[t] = w[t];
+                W[8] = 0x80000000u;
+#pragma unroll
+                for (int t = 9; t < 15; t++) W[t] = 0;
+                W[15] = 256u;
+#pragma unroll
+                for (int part = 0; part < 3; part++) {
+#pragma unroll
+                    for (int j = 0; j < 16; j++) {
+                        const int t = 16 + part * 16 + j;
+                        const uint32_t x =
+                            W[t & 15] + sched_s0(W[(t - 15) & 15]) + W[(t - 7) & 15] + sched_s1(W[(t - 2) & 15]);
+                        W[t & 15] = x;
+                        kw[t - 16][lane] = x + poh_k(t);
+                    }
+                    asm volatile("bar.sync %0, 64;" ::"r"(part + 1) : "memory");
+                }
+                asm volatile("bar.sync 4, 64;" ::: "memory");
+#pragma unroll
+                for (int t = 0; t < 8; t++) w[t] = hout[t][lane];
+            }
+        } else {
+#pragma unroll 1
+            for (uint64_t k = 0; k < r; k++) {
+                uint32_t a = iv[0], b = iv[1], c = iv[2], d = iv[3], e = iv[4], f = iv[5], g = iv[6], h = iv[7];
+#pragma unroll
+                for (int t = 0; t < 64; t++) {
+                    if (t == 16 || t == 32 || t == 48) asm volatile("bar.sync %0, 64;" ::"r"(t / 16) : "memory");
+                    uint32_t x;
+                    if (t < 8) x = w[t] + poh_k(t);
+                    else if (t < 16) x = (t == 8 ? 0x80000000u : t == 15 ? 256u : 0u) + poh_k(t);
+                    else x = kw[t - 16][lane];
+                    const uint32_t t1 =
+                        h + (POH_ROTR(e, 6) ^ POH_ROTR(e, 11) ^ POH_ROTR(e, 25)) + ((e & f) ^ (~e & g)) + x;
+                    const uint32_t t2 = (POH_ROTR(a, 2) ^ POH_ROTR(a, 13) ^ POH_ROTR(a, 22)) + ((a & b) | (c & (a | b)));
+                    h = g;
+                    g = f;
+                    f = e;
+                    e = d + t1;
+                    d = c;
+                    c = b;
+                    b = a;
+                    a = t1 + t2;
+                }
+                if (!done) {
+                    w[0] = iv[0] + a; w[1] = iv[1] + b; w[2] = iv[2] + c; w[3] = iv[3] + d;
+                    w[4] = iv[4] + e; w[5] = iv[5] + f; w[6] = iv[6] + g; w[7] = iv[7] + h;
+                }
+#pragma unroll
+                for (int t = 0; t < 8; t++) hout[t][lane] = w[t];
+                asm volatile("bar.sync 4, 64;" ::: "memory");
+            }
+            if (!done) rem -= r;
+        }
+    }
+}
+
 }  // namespace
 
 size_t poh_batch_workspace_size(uint64_t n) { return sizeof(PohBatchScratch) + 4ull * (n ? n : 1); }
@@ -140,17 +265,24 @@ cudaError_t launch_poh_batch(uint8_t* hashes, const uint64_t* counts, uint64_t n
     poh_hist_kernel<<<blocks, 256, 0, s>>>(counts, n, sc);
     poh_scan_kernel<<<1, 32, 0, s>>>(sc);
     poh_scatter_kernel<<<blocks, 256, 0, s>>>(counts, n, sc);
-    // every warp is independent; block_warps only decides how warps are
-    // packed onto SMs (1: spread over as many SMs as possible; 4: one warp per
-    // sub-partition on as few SMs as possible, leaving the rest to other work)
-    if (block_warps != 4) block_warps = 1;
+    // block_warps 1: independent warps spread over as many SMs as possible;
+    // 4: independent warps packed one per sub-partition on as few SMs as
+    // possible (leaves the rest to other work); 2: paired warps (schedule +
+    // rounds) per 32 lanes, poh_pair_persistent_kernel
+    if (block_warps != 4 && block_warps != 2) block_warps = 1;
     uint64_t need = (n + 31) / 32;
     uint64_t nwarps = need < (uint64_t)warps ? need : (uint64_t)warps;
     unsigned grid = (unsigned)((nwarps + block_warps - 1) / block_warps);
-    if (block_warps == 4)
+    if (block_warps == 4) {
         poh_persistent_kernel<4><<<grid, 128, 0, s>>>(hashes, counts, (uint32_t)n, sc, 1u);
-    else
+    } else if (block_warps == 2) {
+        // pairs: `warps` counts both warps of every pair
+        const uint64_t pairs_max = (uint64_t)(warps / 2 > 0 ? warps / 2 : 1);
+        const unsigned pairs = (unsigned)(need < pairs_max ? need : pairs_max);
+        poh_pair_persistent_kernel<<<pairs, 64, 0, s>>>(hashes, counts, (uint32_t)n, sc);
+    } else {
         poh_persistent_kernel<1><<<grid, 32, 0, s>>>(hashes, counts, (uint32_t)n, sc, 1u);
+    }
     return cudaGetLastError();
 }
 

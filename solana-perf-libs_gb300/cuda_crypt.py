@@ -122,6 +122,10 @@ class CudaCrypt:
         L.gb300_poh_verify_batch_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
                                                     ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
         L.gb300_crypt_tuning.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+        L.gb300_poh_verify_batch_shape.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                                                   ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int,
+                                                   ctypes.c_void_p]
+        L.gb300_poh_verify_batch_shape.restype = ctypes.c_int
 
     # ---- reference entry points ------------------------------------------
     def init(self) -> bool:
@@ -244,6 +248,14 @@ class CudaCrypt:
                                                     stream)
         if rc != 0:
             raise RuntimeError(f"gb300_poh_verify_batch_device: cudaError {rc}")
+
+    def poh_verify_batch_shape(self, hashes, num_hashes, workspace, warps, block_warps, stream=0) -> None:
+        """Device PoH batch with a forced persistent launch shape (diagnostic)."""
+        rc = self.lib.gb300_poh_verify_batch_shape(hashes.data_ptr(), num_hashes.data_ptr(), num_hashes.numel(),
+                                                   workspace.data_ptr(), workspace.numel() * workspace.element_size(),
+                                                   warps, block_warps, stream)
+        if rc != 0:
+            raise RuntimeError(f"gb300_poh_verify_batch_shape: cudaError {rc}")
 
     def ed25519_batch_device(self, packets, v, v_out, s, s_out, queue_word, stream=0) -> None:
         """v / s: 4 device int32 tensors (lens, pubkey, sig-or-privkey, message offsets)."""

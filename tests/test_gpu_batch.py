@@ -122,4 +122,34 @@ def test_tuning_report(lib):
     t = lib.tuning()
     assert t["sig_threads"] in (64, 128, 256)
     assert t["poh_warps_per_smsp"] in (1, 2)
+    assert t["poh_paired"] in (0, 1)
     assert t["sms"] > 0
+
+
+@pytest.mark.parametrize("block_warps,warps_per_sm", [(1, 4), (1, 8), (2, 4), (2, 8), (4, 4), (1, 1)])
+def test_poh_batch_every_launch_shape(lib, oracle, block_warps, warps_per_sm):
+    """Single, paired and packed persistent forms, at several residencies,
+    give the oracle's chains (ragged and zero counts, more chains than
+    resident lanes so lanes refill)."""
+    torch = pytest.importorskip("torch")
+    h, cnt = workloads.poh_ragged(n=25000, max_hashes=400, seed=68 + block_warps)
+    cnt[:5] = [0, 0, 1, 400, 2]
+    exp = oracle.poh_verify_many(h, cnt, nthreads())
+    sms = lib.tuning()["sms"]
+    dh = torch.from_numpy(h.copy()).cuda()
+    dc = torch.from_numpy(cnt.astype(np.int64)).cuda()
+    ws = torch.empty(lib.poh_batch_workspace_size(len(cnt)), dtype=torch.uint8, device="cuda")
+    lib.poh_verify_batch_shape(dh, dc, ws, warps_per_sm * sms, block_warps,
+                               torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(dh.cpu().numpy(), exp)
+
+
+def test_poh_batch_shape_rejects_bad_shapes(lib):
+    torch = pytest.importorskip("torch")
+    dh = torch.zeros((4, 32), dtype=torch.uint8, device="cuda")
+    dc = torch.ones(4, dtype=torch.int64, device="cuda")
+    ws = torch.empty(lib.poh_batch_workspace_size(4), dtype=torch.uint8, device="cuda")
+    for warps, bw in ((0, 1), (64, 3), (10 ** 6, 1)):
+        with pytest.raises(RuntimeError):
+            lib.poh_verify_batch_shape(dh, dc, ws, warps, bw)
