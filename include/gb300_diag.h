@@ -22,13 +22,16 @@ int gb300_int_peak_launch(int kind, uint32_t blocks, uint32_t threads, uint32_t 
                           void* stream);
 
 /* gb300_poh_verify_batch_device with the launch shape forced instead of
- * tuned: `warps` resident warps (1 .. 64 x SM count) of the persistent
- * kernel, packed `block_warps` per block: 1 (one warp per 32 chains),
- * 2 (paired schedule and round warps per 32 chains) or 4 (four single warps
- * per block).  Same results as every other PoH entry point; used to test
- * and time each form.  Returns a cudaError_t. */
+ * tuned: `warps` resident warps (1 .. 64 x SM count; a pair counts two) of
+ * the persistent kernel in form
+ *   0  one warp per 32 chains, one warp per block
+ *   1  one warp per 32 chains, four warps per block
+ *   2  a schedule warp and a round warp per 32 chains, one pair per block
+ *   3  two such pairs per block.
+ * Same results as every other PoH entry point; used to test and time each
+ * form.  Returns a cudaError_t. */
 int gb300_poh_verify_batch_shape(uint8_t* hashes, const uint64_t* num_hashes, uint64_t num_elems, void* workspace,
-                                 size_t workspace_bytes, int warps, int block_warps, void* stream);
+                                 size_t workspace_bytes, int warps, int form, void* stream);
 
 #ifdef __cplusplus
 }

@@ -87,9 +87,9 @@ struct Tuning {
     int sig_threads = 128;        // threads per block of the persistent sign/verify kernel
     int sig_blocks_per_sm = 0;    // 0 = as many as fit
     int poh_warps_per_smsp = 1;   // resident warps of the persistent PoH kernel per SM sub-partition
-    int poh_block_warps = 1;      // 1: one warp per 32 lanes; 2: paired schedule + round warps
+    int poh_form = kPohSingle;    // PohBatchForm of ragged PoH batches
     double sig_ms[3] = {0, 0, 0}; // calibration times for 64 / 128 / 256 threads
-    double poh_ms[3] = {0, 0, 0}; // calibration: single 1 and 2 warps per sub-partition, paired
+    double poh_ms[4] = {0, 0, 0, 0};  // calibration: single and paired forms, 1 and 2 warps per sub-partition
     int calib_sigs = 0, calib_chains = 0;
 };
 
@@ -359,18 +359,18 @@ void tune_device(Device& D) {
         cudaMemcpyAsync(dh, hh.data(), hh.size(), cudaMemcpyHostToDevice, s);
         cudaMemcpyAsync(dc, hc.data(), 8ull * nc, cudaMemcpyHostToDevice, s);
         double best = 1e30;
-        const int mode_wps[3] = {1, 2, 1}, mode_bw[3] = {1, 1, 2};
-        for (int m = 0; m < 3; m++) {
+        const int mode_wps[4] = {1, 2, 1, 2}, mode_form[4] = {kPohSingle, kPohSingle, kPohPair, kPohPair};
+        for (int m = 0; m < 4; m++) {
             cudaError_t err = cudaSuccess;
-            launch_poh_batch(dh, dc, nc, ws, 4 * sms * mode_wps[m], s, mode_bw[m]);   // warm
+            launch_poh_batch(dh, dc, nc, ws, 4 * sms * mode_wps[m], s, mode_form[m]);   // warm
             cudaStreamSynchronize(s);
             float ms = time_ms(
-                s, [&]() { return launch_poh_batch(dh, dc, nc, ws, 4 * sms * mode_wps[m], s, mode_bw[m]); }, err);
+                s, [&]() { return launch_poh_batch(dh, dc, nc, ws, 4 * sms * mode_wps[m], s, mode_form[m]); }, err);
             T.poh_ms[m] = ms;
             if (err == cudaSuccess && ms < best) {
                 best = ms;
                 T.poh_warps_per_smsp = mode_wps[m];
-                T.poh_block_warps = mode_bw[m];
+                T.poh_form = mode_form[m];
             }
         }
         T.calib_chains = (int)nc;
@@ -381,9 +381,10 @@ void tune_device(Device& D) {
     T.sig_threads = env_int("GB300_CRYPT_SIG_THREADS", T.sig_threads);
     T.sig_blocks_per_sm = env_int("GB300_CRYPT_SIG_BLOCKS", T.sig_blocks_per_sm);
     T.poh_warps_per_smsp = env_int("GB300_CRYPT_POH_WARPS_PER_SMSP", T.poh_warps_per_smsp);
-    T.poh_block_warps = env_int("GB300_CRYPT_POH_PAIRED", T.poh_block_warps == 2) ? 2 : 1;
-    LOG("tuned gpu %d: sig threads %d (ms %.3f %.3f %.3f), poh warps/smsp %d (ms %.3f %.3f)\n", D.id, T.sig_threads,
-        T.sig_ms[0], T.sig_ms[1], T.sig_ms[2], T.poh_warps_per_smsp, T.poh_ms[0], T.poh_ms[1]);
+    T.poh_form = env_int("GB300_CRYPT_POH_PAIRED", T.poh_form == kPohPair) ? kPohPair : kPohSingle;
+    LOG("tuned gpu %d: sig threads %d (ms %.3f %.3f %.3f), poh warps/smsp %d %s (ms %.3f %.3f %.3f %.3f)\n", D.id,
+        T.sig_threads, T.sig_ms[0], T.sig_ms[1], T.sig_ms[2], T.poh_warps_per_smsp,
+        T.poh_form == kPohPair ? "paired" : "single", T.poh_ms[0], T.poh_ms[1], T.poh_ms[2], T.poh_ms[3]);
 }
 
 Device* current_device() {
@@ -762,11 +763,11 @@ int gb300_crypt_tuning(char* buf, size_t len) {
                      "{\"device\": %d, \"sms\": %d, \"sig_threads\": %d, \"sig_blocks_per_sm\": %d, "
                      "\"sig_calibration_ms\": {\"64\": %.4f, \"128\": %.4f, \"256\": %.4f}, "
                      "\"sig_calibration_items\": %d, \"poh_warps_per_smsp\": %d, \"poh_paired\": %d, "
-                     "\"poh_calibration_ms\": {\"single_1\": %.4f, \"single_2\": %.4f, \"paired\": %.4f}, "
-                     "\"poh_calibration_chains\": %d}",
+                     "\"poh_calibration_ms\": {\"single_1\": %.4f, \"single_2\": %.4f, \"paired_1\": %.4f, "
+                     "\"paired_2\": %.4f}, \"poh_calibration_chains\": %d}",
                      D->id, D->sms, T.sig_threads, T.sig_blocks_per_sm, T.sig_ms[0], T.sig_ms[1], T.sig_ms[2],
-                     T.calib_sigs, T.poh_warps_per_smsp, T.poh_block_warps == 2, T.poh_ms[0], T.poh_ms[1],
-                     T.poh_ms[2], T.calib_chains);
+                     T.calib_sigs, T.poh_warps_per_smsp, T.poh_form == kPohPair, T.poh_ms[0], T.poh_ms[1],
+                     T.poh_ms[2], T.poh_ms[3], T.calib_chains);
     return n < 0 ? 0 : (n < (int)len ? n : (int)len - 1);
 }
 
@@ -790,19 +791,19 @@ int gb300_poh_verify_batch_device(uint8_t* hashes, const uint64_t* num_hashes, u
     if (!D) return (int)cudaErrorNoDevice;
     const Tuning& T = tuning_for(*D);
     return (int)launch_poh_batch(hashes, num_hashes, num_elems, workspace, 4 * D->sms * T.poh_warps_per_smsp,
-                                 static_cast<cudaStream_t>(stream), T.poh_block_warps);
+                                 static_cast<cudaStream_t>(stream), T.poh_form);
 }
 
 int gb300_poh_verify_batch_shape(uint8_t* hashes, const uint64_t* num_hashes, uint64_t num_elems, void* workspace,
-                                 size_t workspace_bytes, int warps, int block_warps, void* stream) {
+                                 size_t workspace_bytes, int warps, int form, void* stream) {
     if (num_elems == 0) return 0;
     if (int rc = poh_batch_device_checks(hashes, num_hashes, num_elems, workspace, workspace_bytes)) return rc;
-    if (block_warps != 1 && block_warps != 2 && block_warps != 4) return (int)cudaErrorInvalidValue;
+    if (form < kPohSingle || form > kPohPackedPair) return (int)cudaErrorInvalidValue;
     Device* D = current_device();
     if (!D) return (int)cudaErrorNoDevice;
     if (warps < 1 || warps > 64 * D->sms) return (int)cudaErrorInvalidValue;
     return (int)launch_poh_batch(hashes, num_hashes, num_elems, workspace, warps, static_cast<cudaStream_t>(stream),
-                                 block_warps);
+                                 form);
 }
 
 int gb300_poh_verify_batch(uint8_t* hashes, const uint64_t* num_hashes_arr, size_t num_elems) {
@@ -826,9 +827,9 @@ int gb300_poh_verify_batch(uint8_t* hashes, const uint64_t* num_hashes_arr, size
         const uint64_t* dc = reinterpret_cast<const uint64_t*>(d + hb);
         TRY(cudaMemcpyAsync(d, st, hb + cb, cudaMemcpyHostToDevice, s));
         std::vector<uint64_t> key = {num_elems, (uint64_t)(uintptr_t)d, (uint64_t)(uintptr_t)Q.d_scratch.p,
-                                     (uint64_t)warps, (uint64_t)T.poh_block_warps};
+                                     (uint64_t)warps, (uint64_t)T.poh_form};
         TRY(run_graph(Q.g_poh, key, s, [&](cudaStream_t cs) {
-            return launch_poh_batch(d, dc, num_elems, Q.d_scratch.p, warps, cs, T.poh_block_warps);
+            return launch_poh_batch(d, dc, num_elems, Q.d_scratch.p, warps, cs, T.poh_form);
         }));
         TRY(cudaMemcpyAsync(st, d, hb, cudaMemcpyDeviceToHost, s));
         TRY(cudaStreamSynchronize(s));

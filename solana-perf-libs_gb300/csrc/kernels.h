@@ -44,9 +44,15 @@ cudaError_t launch_poh_verify(uint8_t* hashes, const uint64_t* num_hashes, uint6
 // Ragged PoH batch in one persistent launch (poh_batch.cu): entries ordered
 // longest first, `warps` resident warps refilling lanes from a queue.
 // `workspace` holds poh_batch_workspace_size(n) bytes of device memory.
+enum PohBatchForm : int {
+    kPohSingle = 0,         // one warp per 32 chains, one warp per block
+    kPohPackedSingle = 1,   // one warp per 32 chains, four warps per block (fewer SMs)
+    kPohPair = 2,           // schedule warp + round warp per 32 chains, one pair per block
+    kPohPackedPair = 3,     // two such pairs per block (fewer SMs)
+};
 size_t poh_batch_workspace_size(uint64_t n);
 cudaError_t launch_poh_batch(uint8_t* hashes, const uint64_t* counts, uint64_t n, void* workspace, int warps,
-                             cudaStream_t s, int block_warps = 1);
+                             cudaStream_t s, int form = kPohSingle);
 
 // Mixed verify + sign work for one persistent launch (sig_batch.cu).  Both
 // batches index the same packet buffer.  Verify items are chunks

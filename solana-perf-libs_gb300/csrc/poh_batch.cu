@@ -73,13 +73,34 @@ __device__ __forceinline__ void store_entry(uint8_t* hashes, uint32_t e, const u
     p[1] = make_uint4(bswap_u32(w[4]), bswap_u32(w[5]), bswap_u32(w[6]), bswap_u32(w[7]));
 }
 
-// BW warps per block, each compiled for exactly its block size (a kernel
-// bounded for 128 threads but launched with 32 ran 24% slower).
+struct HashWords {
+    uint32_t v[8];
+};
+
+// The hashing loops of the persistent kernels are separate non-inlined
+// functions.  Compiled inline, their schedule depended on the code around
+// them: the single-warp loop ran at ~2,550 cycles per hash in a 32-thread
+// block but ~3,150 in a 128-thread one, and the paired loop ~2,570 inside
+// the queue loop against ~2,180 in poh.cu's poh_pair_kernel.  Compiled
+// alone they run the same in every kernel that calls them.
+static __device__ __noinline__ HashWords single_run(HashWords in, uint64_t r, uint32_t one) {
+    const PohMul M(one);
+    uint32_t w[8];
+#pragma unroll
+    for (int t = 0; t < 8; t++) w[t] = in.v[t];
+#pragma unroll 1
+    for (uint64_t k = 0; k < r; k++) poh_step_mix<0, 0, 0>(w, M);
+    HashWords out;
+#pragma unroll
+    for (int t = 0; t < 8; t++) out.v[t] = w[t];
+    return out;
+}
+
+// BW independent warps per block.
 template <int BW>
 __global__ void __launch_bounds__(32 * BW) poh_persistent_kernel(uint8_t* hashes, const uint64_t* counts, uint32_t n,
                                                                  PohBatchScratch* s, uint32_t one) {
     const uint32_t lane = threadIdx.x & 31u;
-    const PohMul M(one);
     uint32_t w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     uint64_t rem = 0;
     uint32_t cur = 0xffffffffu;
@@ -118,44 +139,129 @@ __global__ void __launch_bounds__(32 * BW) poh_persistent_kernel(uint8_t* hashes
             r = other < r ? other : r;
         }
         if (!done) {
-#pragma unroll 1
-            for (uint64_t k = 0; k < r; k++) poh_step_mix<0, 0, 0>(w, M);
+            HashWords h;
+#pragma unroll
+            for (int t = 0; t < 8; t++) h.v[t] = w[t];
+            h = single_run(h, r, one);
+#pragma unroll
+            for (int t = 0; t < 8; t++) w[t] = h.v[t];
             rem -= r;
         }
     }
 }
 
-// Paired form: two warps per 32 lanes, as in poh.cu's poh_pair_kernel (warp
-// 1 computes the message schedule into shared memory while warp 0 runs the
-// rounds), inside the persistent longest-first loop.  Warp 0 owns the queue:
-// each refill round it stores finished chains, loads new ones and the step
-// count r (the smallest remaining count among its busy lanes), and hands the
-// current hash words and r to warp 1 through shared memory at barrier 5;
-// then both run r hashes with barriers 1-4 per hash.  r == 0 means every
-// lane is done and both warps leave together.
+// Paired form: two warps per 32 lanes, as in poh.cu's poh_pair_kernel (the
+// schedule warp computes the message schedule into shared memory while the
+// round warp runs the rounds), inside the persistent longest-first loop.
+// The round warp owns the queue: each refill round it stores finished
+// chains, loads new ones and the step count r (the smallest remaining count
+// among its busy lanes), and hands the current hash words and r to the
+// schedule warp through shared memory at the pair's fifth barrier; then both
+// run r hashes with the pair's barriers 1-4 per hash.  r == 0 means every
+// lane is done and both warps leave together.  A block holds P pairs; pair
+// p uses named barriers 6p+1 .. 6p+5 (64 threads each) and its own slices
+// of the shared arrays, so pairs never wait on one another.
+constexpr int kMaxPairsPerBlock = 2;
+__shared__ uint32_t pair_kw[kMaxPairsPerBlock][48][32];   // K[t] + W[t], t = 16..63, per lane
+__shared__ uint32_t pair_hout[kMaxPairsPerBlock][8][32];  // hash words, round warp -> schedule warp
+
 __device__ __forceinline__ uint32_t sched_s0(uint32_t x) { return POH_ROTR(x, 7) ^ POH_ROTR(x, 18) ^ (x >> 3); }
 __device__ __forceinline__ uint32_t sched_s1(uint32_t x) { return POH_ROTR(x, 17) ^ POH_ROTR(x, 19) ^ (x >> 10); }
 
-__global__ void __launch_bounds__(64) poh_pair_persistent_kernel(uint8_t* hashes, const uint64_t* counts, uint32_t n,
-                                                                 PohBatchScratch* s) {
-    __shared__ uint32_t kw[48][32];
-    __shared__ uint32_t hout[8][32];
-    __shared__ uint64_t run_len;
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+// round warp of pair PI: r hashes of its 32 chains; a lane keeps its words
+// after its first `lim` hashes (lim = 0 for a lane with no chain)
+template <int PI>
+static __device__ __noinline__ HashWords pair_rounds(HashWords in, uint32_t lane, uint64_t r, uint64_t lim) {
     const uint32_t iv[8] = {0x6a09e667u, 0xbb67ae85u, 0x3c6ef372u, 0xa54ff53au,
                             0x510e527fu, 0x9b05688cu, 0x1f83d9abu, 0x5be0cd19u};
-    uint32_t w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    uint32_t w[8];
+#pragma unroll
+    for (int t = 0; t < 8; t++) w[t] = in.v[t];
+#pragma unroll 1
+    for (uint64_t k = 0; k < r; k++) {
+        uint32_t a = iv[0], b = iv[1], c = iv[2], d = iv[3], e = iv[4], f = iv[5], g = iv[6], h = iv[7];
+#pragma unroll
+        for (int t = 0; t < 64; t++) {
+            if (t == 16 || t == 32 || t == 48) asm volatile("bar.sync %0, 64;" ::"r"(6 * PI + t / 16) : "memory");
+            uint32_t x;
+            if (t < 8) x = w[t] + poh_k(t);
+            else if (t < 16) x = (t == 8 ? 0x80000000u : t == 15 ? 256u : 0u) + poh_k(t);
+            else x = pair_kw[PI][t - 16][lane];
+            const uint32_t t1 = h + (POH_ROTR(e, 6) ^ POH_ROTR(e, 11) ^ POH_ROTR(e, 25)) + ((e & f) ^ (~e & g)) + x;
+            const uint32_t t2 = (POH_ROTR(a, 2) ^ POH_ROTR(a, 13) ^ POH_ROTR(a, 22)) + ((a & b) | (c & (a | b)));
+            h = g;
+            g = f;
+            f = e;
+            e = d + t1;
+            d = c;
+            c = b;
+            b = a;
+            a = t1 + t2;
+        }
+        const bool live = k < lim;
+        w[0] = live ? iv[0] + a : w[0]; w[1] = live ? iv[1] + b : w[1];
+        w[2] = live ? iv[2] + c : w[2]; w[3] = live ? iv[3] + d : w[3];
+        w[4] = live ? iv[4] + e : w[4]; w[5] = live ? iv[5] + f : w[5];
+        w[6] = live ? iv[6] + g : w[6]; w[7] = live ? iv[7] + h : w[7];
+#pragma unroll
+        for (int t = 0; t < 8; t++) pair_hout[PI][t][lane] = w[t];
+        asm volatile("bar.sync %0, 64;" ::"n"(6 * PI + 4) : "memory");
+    }
+    HashWords out;
+#pragma unroll
+    for (int t = 0; t < 8; t++) out.v[t] = w[t];
+    return out;
+}
+
+// schedule warp of pair PI: the message schedule of r hashes, each from the
+// hash words the round warp published at barrier 4 of the previous hash
+template <int PI>
+static __device__ __noinline__ void pair_schedule(HashWords in, uint32_t lane, uint64_t r) {
+    uint32_t w[8];
+#pragma unroll
+    for (int t = 0; t < 8; t++) w[t] = in.v[t];
+#pragma unroll 1
+    for (uint64_t k = 0; k < r; k++) {
+        uint32_t W[16];
+#pragma unroll
+        for (int t = 0; t < 8; t++) W[t] = w[t];
+        W[8] = 0x80000000u;
+#pragma unroll
+        for (int t = 9; t < 15; t++) W[t] = 0;
+        W[15] = 256u;
+#pragma unroll
+        for (int part = 0; part < 3; part++) {
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+                const int t = 16 + part * 16 + j;
+                const uint32_t x = W[t & 15] + sched_s0(W[(t - 15) & 15]) + W[(t - 7) & 15] + sched_s1(W[(t - 2) & 15]);
+                W[t & 15] = x;
+                pair_kw[PI][t - 16][lane] = x + poh_k(t);
+            }
+            asm volatile("bar.sync %0, 64;" ::"r"(6 * PI + 1 + part) : "memory");
+        }
+        asm volatile("bar.sync %0, 64;" ::"n"(6 * PI + 4) : "memory");
+#pragma unroll
+        for (int t = 0; t < 8; t++) w[t] = pair_hout[PI][t][lane];
+    }
+}
+
+template <int PI>
+__device__ __forceinline__ void pair_persistent(uint8_t* hashes, const uint64_t* counts, uint32_t n,
+                                                PohBatchScratch* s, uint64_t* run_len, uint32_t role) {
+    const uint32_t lane = threadIdx.x & 31u;
+    HashWords w = {{0, 0, 0, 0, 0, 0, 0, 0}};
     uint64_t rem = 0;
     uint32_t cur = 0xffffffffu;
     bool done = false;
     for (;;) {
-        if (warp == 0) {
+        if (role == 0) {
             for (;;) {
                 const bool need = !done && rem == 0;
                 const uint32_t mask = __ballot_sync(0xffffffffu, need);
                 if (mask == 0) break;
                 if (need && cur != 0xffffffffu) {
-                    store_entry(hashes, cur, w);
+                    store_entry(hashes, cur, w.v);
                     cur = 0xffffffffu;
                 }
                 uint32_t base = 0;
@@ -167,7 +273,7 @@ __global__ void __launch_bounds__(64) poh_pair_persistent_kernel(uint8_t* hashes
                         done = true;
                     } else {
                         cur = s->order[k];
-                        load_entry(hashes, cur, w);
+                        load_entry(hashes, cur, w.v);
                         rem = counts[cur];
                     }
                 }
@@ -180,74 +286,33 @@ __global__ void __launch_bounds__(64) poh_pair_persistent_kernel(uint8_t* hashes
             }
             if (r == ~0ull) r = 0;
 #pragma unroll
-            for (int t = 0; t < 8; t++) hout[t][lane] = w[t];
-            if (lane == 0) run_len = r;
+            for (int t = 0; t < 8; t++) pair_hout[PI][t][lane] = w.v[t];
+            if (lane == 0) *run_len = r;
         }
-        asm volatile("bar.sync 5, 64;" ::: "memory");
-        const uint64_t r = run_len;
+        asm volatile("bar.sync %0, 64;" ::"n"(6 * PI + 5) : "memory");
+        const uint64_t r = *run_len;
         if (r == 0) break;
-        if (warp == 1) {
+        if (role == 1) {
+            HashWords h0;
 #pragma unroll
-            for (int t = 0; t < 8; t++) w[t] = hout[t][lane];
-#pragma unroll 1
-            for (uint64_t k = 0; k < r; k++) {
-                uint32_t W[16];
-#pragma unroll
-                for (int t = 0; t < 8; t++) W[t] = w[t];
-                W[8] = 0x80000000u;
-#pragma unroll
-                for (int t = 9; t < 15; t++) W[t] = 0;
-                W[15] = 256u;
-#pragma unroll
-                for (int part = 0; part < 3; part++) {
-#pragma unroll
-                    for (int j = 0; j < 16; j++) {
-                        const int t = 16 + part * 16 + j;
-                        const uint32_t x =
-                            W[t & 15] + sched_s0(W[(t - 15) & 15]) + W[(t - 7) & 15] + sched_s1(W[(t - 2) & 15]);
-                        W[t & 15] = x;
-                        kw[t - 16][lane] = x + poh_k(t);
-                    }
-                    asm volatile("bar.sync %0, 64;" ::"r"(part + 1) : "memory");
-                }
-                asm volatile("bar.sync 4, 64;" ::: "memory");
-#pragma unroll
-                for (int t = 0; t < 8; t++) w[t] = hout[t][lane];
-            }
+            for (int t = 0; t < 8; t++) h0.v[t] = pair_hout[PI][t][lane];
+            pair_schedule<PI>(h0, lane, r);
         } else {
-#pragma unroll 1
-            for (uint64_t k = 0; k < r; k++) {
-                uint32_t a = iv[0], b = iv[1], c = iv[2], d = iv[3], e = iv[4], f = iv[5], g = iv[6], h = iv[7];
-#pragma unroll
-                for (int t = 0; t < 64; t++) {
-                    if (t == 16 || t == 32 || t == 48) asm volatile("bar.sync %0, 64;" ::"r"(t / 16) : "memory");
-                    uint32_t x;
-                    if (t < 8) x = w[t] + poh_k(t);
-                    else if (t < 16) x = (t == 8 ? 0x80000000u : t == 15 ? 256u : 0u) + poh_k(t);
-                    else x = kw[t - 16][lane];
-                    const uint32_t t1 =
-                        h + (POH_ROTR(e, 6) ^ POH_ROTR(e, 11) ^ POH_ROTR(e, 25)) + ((e & f) ^ (~e & g)) + x;
-                    const uint32_t t2 = (POH_ROTR(a, 2) ^ POH_ROTR(a, 13) ^ POH_ROTR(a, 22)) + ((a & b) | (c & (a | b)));
-                    h = g;
-                    g = f;
-                    f = e;
-                    e = d + t1;
-                    d = c;
-                    c = b;
-                    b = a;
-                    a = t1 + t2;
-                }
-                if (!done) {
-                    w[0] = iv[0] + a; w[1] = iv[1] + b; w[2] = iv[2] + c; w[3] = iv[3] + d;
-                    w[4] = iv[4] + e; w[5] = iv[5] + f; w[6] = iv[6] + g; w[7] = iv[7] + h;
-                }
-#pragma unroll
-                for (int t = 0; t < 8; t++) hout[t][lane] = w[t];
-                asm volatile("bar.sync 4, 64;" ::: "memory");
-            }
+            w = pair_rounds<PI>(w, lane, r, done ? 0 : r);
             if (!done) rem -= r;
         }
     }
+}
+
+// P pairs per block: warps 2p (rounds, queue) and 2p + 1 (schedule)
+template <int P>
+__global__ void __launch_bounds__(64 * P) poh_pair_persistent_kernel(uint8_t* hashes, const uint64_t* counts,
+                                                                     uint32_t n, PohBatchScratch* s) {
+    static_assert(P >= 1 && P <= kMaxPairsPerBlock, "pairs per block");
+    __shared__ uint64_t run_len[P];
+    const uint32_t warp = threadIdx.x >> 5, pair = warp >> 1, role = warp & 1u;
+    if (pair == 0) pair_persistent<0>(hashes, counts, n, s, &run_len[0], role);
+    else if (P > 1) pair_persistent<1>(hashes, counts, n, s, &run_len[P > 1 ? 1 : 0], role);
 }
 
 }  // namespace
@@ -255,7 +320,7 @@ __global__ void __launch_bounds__(64) poh_pair_persistent_kernel(uint8_t* hashes
 size_t poh_batch_workspace_size(uint64_t n) { return sizeof(PohBatchScratch) + 4ull * (n ? n : 1); }
 
 cudaError_t launch_poh_batch(uint8_t* hashes, const uint64_t* counts, uint64_t n, void* workspace,
-                             int warps, cudaStream_t s, int block_warps) {
+                             int warps, cudaStream_t s, int form) {
     if (n == 0) return cudaSuccess;
     if (n > 0xffffffffull) return cudaErrorInvalidValue;
     PohBatchScratch* sc = static_cast<PohBatchScratch*>(workspace);
@@ -265,23 +330,24 @@ cudaError_t launch_poh_batch(uint8_t* hashes, const uint64_t* counts, uint64_t n
     poh_hist_kernel<<<blocks, 256, 0, s>>>(counts, n, sc);
     poh_scan_kernel<<<1, 32, 0, s>>>(sc);
     poh_scatter_kernel<<<blocks, 256, 0, s>>>(counts, n, sc);
-    // block_warps 1: independent warps spread over as many SMs as possible;
-    // 4: independent warps packed one per sub-partition on as few SMs as
-    // possible (leaves the rest to other work); 2: paired warps (schedule +
-    // rounds) per 32 lanes, poh_pair_persistent_kernel
-    if (block_warps != 4 && block_warps != 2) block_warps = 1;
-    uint64_t need = (n + 31) / 32;
-    uint64_t nwarps = need < (uint64_t)warps ? need : (uint64_t)warps;
-    unsigned grid = (unsigned)((nwarps + block_warps - 1) / block_warps);
-    if (block_warps == 4) {
-        poh_persistent_kernel<4><<<grid, 128, 0, s>>>(hashes, counts, (uint32_t)n, sc, 1u);
-    } else if (block_warps == 2) {
-        // pairs: `warps` counts both warps of every pair
-        const uint64_t pairs_max = (uint64_t)(warps / 2 > 0 ? warps / 2 : 1);
-        const unsigned pairs = (unsigned)(need < pairs_max ? need : pairs_max);
-        poh_pair_persistent_kernel<<<pairs, 64, 0, s>>>(hashes, counts, (uint32_t)n, sc);
-    } else {
-        poh_persistent_kernel<1><<<grid, 32, 0, s>>>(hashes, counts, (uint32_t)n, sc, 1u);
+    const uint64_t need = (n + 31) / 32;               // 32-lane groups
+    const uint64_t wmax = (uint64_t)(warps > 0 ? warps : 1);
+    const uint64_t nwarps = need < wmax ? need : wmax;  // single forms: one warp per group
+    const uint64_t pmax = wmax / 2 > 0 ? wmax / 2 : 1;  // paired forms: `warps` counts both warps of a pair
+    const uint64_t pairs = need < pmax ? need : pmax;
+    switch (form) {
+        case kPohPackedSingle:
+            poh_persistent_kernel<4><<<(unsigned)((nwarps + 3) / 4), 128, 0, s>>>(hashes, counts, (uint32_t)n, sc, 1u);
+            break;
+        case kPohPair:
+            poh_pair_persistent_kernel<1><<<(unsigned)pairs, 64, 0, s>>>(hashes, counts, (uint32_t)n, sc);
+            break;
+        case kPohPackedPair:
+            poh_pair_persistent_kernel<2><<<(unsigned)((pairs + 1) / 2), 128, 0, s>>>(hashes, counts, (uint32_t)n, sc);
+            break;
+        default:
+            poh_persistent_kernel<1><<<(unsigned)nwarps, 32, 0, s>>>(hashes, counts, (uint32_t)n, sc, 1u);
+            break;
     }
     return cudaGetLastError();
 }
@@ -349,7 +415,9 @@ extern "C" int gb300_poh_verify_batch_static(uint8_t* hashes, const uint64_t* nu
     }
     // The array keeps the previous call's contents; launch_poh_batch clears
     // the header (bucket counts, cursors, queue head) on every call and
-    // rewrites the entry order in full.  One warp per SM sub-partition, the
-    // shape the autotuner picks on GB300.
-    return (int)launch_poh_batch(hashes, num_hashes, num_elems, scratch, 4 * sms, static_cast<cudaStream_t>(stream));
+    // rewrites the entry order in full.  Paired warps, one warp per SM
+    // sub-partition: the fastest form measured on GB300 (this entry point
+    // runs no autotuning, which would allocate).
+    return (int)launch_poh_batch(hashes, num_hashes, num_elems, scratch, 4 * sms, static_cast<cudaStream_t>(stream),
+                                 kPohPair);
 }

@@ -204,10 +204,11 @@ cudaError_t launch_pohs(gb300_server* sv, Slot& S) {
     }
     uint8_t* d = static_cast<uint8_t*>(S.d_data.p);
     if ((e = cudaMemcpyAsync(d, st, hb + cb, cudaMemcpyHostToDevice, S.stream)) != cudaSuccess) return e;
-    // PoH warps packed four to a block: whole SMs' sub-partitions, not one
-    // sub-partition on every SM, so signature launches keep the other SMs
+    // PoH warps packed four to a block (two schedule + round pairs): whole
+    // SMs' sub-partitions, not one sub-partition on every SM, so signature
+    // launches keep the other SMs
     if ((e = launch_poh_batch(d, reinterpret_cast<const uint64_t*>(d + hb), n, S.d_scratch.p, sv->info.poh_warps,
-                              S.stream, 4)) != cudaSuccess)
+                              S.stream, kPohPackedPair)) != cudaSuccess)
         return e;
     if ((e = cudaMemcpyAsync(st, d, hb, cudaMemcpyDeviceToHost, S.stream)) != cudaSuccess) return e;
     return cudaEventRecord(S.done, S.stream);

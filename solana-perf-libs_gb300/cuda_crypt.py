@@ -249,11 +249,14 @@ class CudaCrypt:
         if rc != 0:
             raise RuntimeError(f"gb300_poh_verify_batch_device: cudaError {rc}")
 
-    def poh_verify_batch_shape(self, hashes, num_hashes, workspace, warps, block_warps, stream=0) -> None:
-        """Device PoH batch with a forced persistent launch shape (diagnostic)."""
+    POH_SINGLE, POH_PACKED_SINGLE, POH_PAIR, POH_PACKED_PAIR = 0, 1, 2, 3
+
+    def poh_verify_batch_shape(self, hashes, num_hashes, workspace, warps, form, stream=0) -> None:
+        """Device PoH batch with a forced persistent launch shape (diagnostic);
+        form: POH_SINGLE, POH_PACKED_SINGLE, POH_PAIR or POH_PACKED_PAIR."""
         rc = self.lib.gb300_poh_verify_batch_shape(hashes.data_ptr(), num_hashes.data_ptr(), num_hashes.numel(),
                                                    workspace.data_ptr(), workspace.numel() * workspace.element_size(),
-                                                   warps, block_warps, stream)
+                                                   warps, form, stream)
         if rc != 0:
             raise RuntimeError(f"gb300_poh_verify_batch_shape: cudaError {rc}")
 

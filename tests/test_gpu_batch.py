@@ -126,21 +126,36 @@ def test_tuning_report(lib):
     assert t["sms"] > 0
 
 
-@pytest.mark.parametrize("block_warps,warps_per_sm", [(1, 4), (1, 8), (2, 4), (2, 8), (4, 4), (1, 1)])
-def test_poh_batch_every_launch_shape(lib, oracle, block_warps, warps_per_sm):
-    """Single, paired and packed persistent forms, at several residencies,
-    give the oracle's chains (ragged and zero counts, more chains than
-    resident lanes so lanes refill)."""
+@pytest.mark.parametrize("form,warps_per_sm", [(0, 4), (0, 8), (0, 1), (1, 4), (2, 4), (2, 8), (2, 2),
+                                               (3, 4), (3, 2)])
+def test_poh_batch_every_launch_shape(lib, oracle, form, warps_per_sm):
+    """Single, packed, paired and packed-paired persistent forms, at several
+    residencies (odd pair counts included), give the oracle's chains (ragged
+    and zero counts, more chains than resident lanes so lanes refill)."""
     torch = pytest.importorskip("torch")
-    h, cnt = workloads.poh_ragged(n=25000, max_hashes=400, seed=68 + block_warps)
+    h, cnt = workloads.poh_ragged(n=25000, max_hashes=400, seed=68 + form)
     cnt[:5] = [0, 0, 1, 400, 2]
     exp = oracle.poh_verify_many(h, cnt, nthreads())
     sms = lib.tuning()["sms"]
     dh = torch.from_numpy(h.copy()).cuda()
     dc = torch.from_numpy(cnt.astype(np.int64)).cuda()
     ws = torch.empty(lib.poh_batch_workspace_size(len(cnt)), dtype=torch.uint8, device="cuda")
-    lib.poh_verify_batch_shape(dh, dc, ws, warps_per_sm * sms, block_warps,
-                               torch.cuda.current_stream().cuda_stream)
+    warps = warps_per_sm * sms + (2 if form >= 2 else 0)   # + one pair: odd pair count per block
+    lib.poh_verify_batch_shape(dh, dc, ws, warps, form, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(dh.cpu().numpy(), exp)
+
+
+@pytest.mark.parametrize("form", [0, 1, 2, 3])
+def test_poh_batch_forms_few_chains(lib, oracle, form):
+    """Fewer chains than one warp (a partly empty pair and block)."""
+    torch = pytest.importorskip("torch")
+    h, cnt = workloads.poh_ragged(n=37, max_hashes=3000, seed=90 + form)
+    exp = oracle.poh_verify_many(h, cnt, nthreads())
+    dh = torch.from_numpy(h.copy()).cuda()
+    dc = torch.from_numpy(cnt.astype(np.int64)).cuda()
+    ws = torch.empty(lib.poh_batch_workspace_size(len(cnt)), dtype=torch.uint8, device="cuda")
+    lib.poh_verify_batch_shape(dh, dc, ws, 608, form, torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
     assert np.array_equal(dh.cpu().numpy(), exp)
 
@@ -150,6 +165,6 @@ def test_poh_batch_shape_rejects_bad_shapes(lib):
     dh = torch.zeros((4, 32), dtype=torch.uint8, device="cuda")
     dc = torch.ones(4, dtype=torch.int64, device="cuda")
     ws = torch.empty(lib.poh_batch_workspace_size(4), dtype=torch.uint8, device="cuda")
-    for warps, bw in ((0, 1), (64, 3), (10 ** 6, 1)):
+    for warps, form in ((0, 0), (64, 4), (64, -1), (10 ** 6, 0)):
         with pytest.raises(RuntimeError):
-            lib.poh_verify_batch_shape(dh, dc, ws, warps, bw)
+            lib.poh_verify_batch_shape(dh, dc, ws, warps, form)
