@@ -671,8 +671,8 @@ def run_ours(args):
                    "l2": "flushed between steps (256 MB write)", "stream": "torch current stream"},
         "roofline": {"bound": "int_alu", "achieved": achieved_ops / 1e12, "peak": peaks["lop3"] / 1e12,
                      "unit": "Tops/s", "frac": achieved_ops / peaks["lop3"],
-                     "traffic": traffic.get("poh_pair_kernel"),
-                     "kernel": "poh_pair_kernel (two warps per 32 chains)",
+                     "traffic": traffic.get("poh_pair_persistent_kernel"),
+                     "kernel": "poh_pair_persistent_kernel<1>, direct mode (two warps per 32 chains)",
                      "ops_per_unit": POH_OPS_PER_HASH,
                      "peak_source": "measured lop3.b32 throughput (gb300_int_peak_launch), 'of measured'",
                      "parallelism_cap": "4096 chains = 128 round warps + 128 schedule warps on 608 SM "

@@ -798,7 +798,7 @@ int gb300_poh_verify_batch_shape(uint8_t* hashes, const uint64_t* num_hashes, ui
                                  size_t workspace_bytes, int warps, int form, void* stream) {
     if (num_elems == 0) return 0;
     if (int rc = poh_batch_device_checks(hashes, num_hashes, num_elems, workspace, workspace_bytes)) return rc;
-    if (form < kPohSingle || form > kPohPackedPair) return (int)cudaErrorInvalidValue;
+    if (form < kPohSingle || form > kPohPairDirect) return (int)cudaErrorInvalidValue;
     Device* D = current_device();
     if (!D) return (int)cudaErrorNoDevice;
     if (warps < 1 || warps > 64 * D->sms) return (int)cudaErrorInvalidValue;

@@ -49,10 +49,14 @@ enum PohBatchForm : int {
     kPohPackedSingle = 1,   // one warp per 32 chains, four warps per block (fewer SMs)
     kPohPair = 2,           // schedule warp + round warp per 32 chains, one pair per block
     kPohPackedPair = 3,     // two such pairs per block (fewer SMs)
+    kPohPairDirect = 4,     // no queue: one pair per 32 consecutive entries (workspace unused)
 };
 size_t poh_batch_workspace_size(uint64_t n);
 cudaError_t launch_poh_batch(uint8_t* hashes, const uint64_t* counts, uint64_t n, void* workspace, int warps,
                              cudaStream_t s, int form = kPohSingle);
+// The direct paired form alone: poh_pair_persistent_kernel without a queue,
+// one block of two warps per 32 consecutive entries.
+cudaError_t launch_poh_pair_direct(uint8_t* hashes, const uint64_t* counts, uint64_t n, cudaStream_t s);
 
 // Mixed verify + sign work for one persistent launch (sig_batch.cu).  Both
 // batches index the same packet buffer.  Verify items are chunks

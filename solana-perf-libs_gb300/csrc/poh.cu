@@ -57,123 +57,23 @@ __global__ void __launch_bounds__(POH_THREADS) poh_verify_kernel(uint8_t* hashes
     poh_chain(hashes + 32 * i, num_hashes[i], one);
 }
 
-// ---------------------------------------------------------------------------
-// Two warps per 32 chains.  A lone warp is bound by its sub-partition's ALU
-// pipe (one warp instruction every 2 cycles, ~1,330 per hash), and a batch of
-// a few thousand chains leaves most sub-partitions idle.  Here warp 1 of the
-// block (on another sub-partition) computes the message schedule K[t] + W[t],
-// t = 16..63, into shared memory while warp 0 runs the 64 rounds: about 840
-// ALU instructions per hash on the round warp instead of ~1,330.  Four named
-// barriers per hash hand the data across (hardware barriers, no spinning):
-//   B1 KW[16..31] ready, B2 KW[32..47], B3 KW[48..63], B4 hash out ready.
-// Both warps loop the same count (the largest of their 32 chains) and
-// execute every barrier; a lane whose chain is shorter stops updating its
-// state (predicated), so ragged counts stay exact.
-__device__ __forceinline__ uint32_t s0w(uint32_t x) { return POH_ROTR(x, 7) ^ POH_ROTR(x, 18) ^ (x >> 3); }
-__device__ __forceinline__ uint32_t s1w(uint32_t x) { return POH_ROTR(x, 17) ^ POH_ROTR(x, 19) ^ (x >> 10); }
-
-__global__ void __launch_bounds__(64) poh_pair_kernel(uint8_t* hashes, const uint64_t* num_hashes, uint64_t n) {
-    __shared__ uint32_t kw[48][32];   // K[t] + W[t], t = 16..63, per lane
-    __shared__ uint32_t hout[8][32];  // hash words handed from the round warp to the schedule warp
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    const uint64_t i = (uint64_t)blockIdx.x * 32 + lane;
-    const bool valid = i < n;
-    const uint64_t mine = valid ? num_hashes[i] : 0;
-    uint64_t cnt = mine;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const uint64_t other = __shfl_xor_sync(0xffffffffu, cnt, o);
-        cnt = other > cnt ? other : cnt;
-    }
-    uint32_t w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    if (valid) {
-        const uint4* p = reinterpret_cast<const uint4*>(hashes + 32 * i);
-        uint4 lo = p[0], hi = p[1];
-        w[0] = bswap(lo.x); w[1] = bswap(lo.y); w[2] = bswap(lo.z); w[3] = bswap(lo.w);
-        w[4] = bswap(hi.x); w[5] = bswap(hi.y); w[6] = bswap(hi.z); w[7] = bswap(hi.w);
-    }
-    const uint32_t iv[8] = {0x6a09e667u, 0xbb67ae85u, 0x3c6ef372u, 0xa54ff53au,
-                            0x510e527fu, 0x9b05688cu, 0x1f83d9abu, 0x5be0cd19u};
-    if (warp == 1) {
-        // ---- schedule warp ----
-#pragma unroll 1
-        for (uint64_t k = 0; k < cnt; k++) {
-            uint32_t W[16];
-#pragma unroll
-            for (int t = 0; t < 8; t++) W[t] = w[t];
-            W[8] = 0x80000000u;
-#pragma unroll
-            for (int t = 9; t < 15; t++) W[t] = 0;
-            W[15] = 256u;
-#pragma unroll
-            for (int part = 0; part < 3; part++) {
-#pragma unroll
-                for (int j = 0; j < 16; j++) {
-                    const int t = 16 + part * 16 + j;
-                    const uint32_t x = W[t & 15] + s0w(W[(t - 15) & 15]) + W[(t - 7) & 15] + s1w(W[(t - 2) & 15]);
-                    W[t & 15] = x;
-                    kw[t - 16][lane] = x + poh_k(t);
-                }
-                asm volatile("bar.sync %0, 64;" ::"r"(part + 1) : "memory");
-            }
-            asm volatile("bar.sync 4, 64;" ::: "memory");
-#pragma unroll
-            for (int t = 0; t < 8; t++) w[t] = hout[t][lane];
-        }
-    } else {
-        // ---- round warp ----
-#pragma unroll 1
-        for (uint64_t k = 0; k < cnt; k++) {
-            uint32_t a = iv[0], b = iv[1], c = iv[2], d = iv[3], e = iv[4], f = iv[5], g = iv[6], h = iv[7];
-#pragma unroll
-            for (int t = 0; t < 64; t++) {
-                if (t == 16 || t == 32 || t == 48) asm volatile("bar.sync %0, 64;" ::"r"(t / 16) : "memory");
-                uint32_t x;
-                if (t < 8) x = w[t] + poh_k(t);
-                else if (t < 16) x = (t == 8 ? 0x80000000u : t == 15 ? 256u : 0u) + poh_k(t);
-                else x = kw[t - 16][lane];
-                const uint32_t t1 = h + (POH_ROTR(e, 6) ^ POH_ROTR(e, 11) ^ POH_ROTR(e, 25)) + ((e & f) ^ (~e & g)) + x;
-                const uint32_t t2 = (POH_ROTR(a, 2) ^ POH_ROTR(a, 13) ^ POH_ROTR(a, 22)) + ((a & b) | (c & (a | b)));
-                h = g;
-                g = f;
-                f = e;
-                e = d + t1;
-                d = c;
-                c = b;
-                b = a;
-                a = t1 + t2;
-            }
-            const bool live = k < mine;
-            w[0] = live ? iv[0] + a : w[0]; w[1] = live ? iv[1] + b : w[1];
-            w[2] = live ? iv[2] + c : w[2]; w[3] = live ? iv[3] + d : w[3];
-            w[4] = live ? iv[4] + e : w[4]; w[5] = live ? iv[5] + f : w[5];
-            w[6] = live ? iv[6] + g : w[6]; w[7] = live ? iv[7] + h : w[7];
-#pragma unroll
-            for (int t = 0; t < 8; t++) hout[t][lane] = w[t];
-            asm volatile("bar.sync 4, 64;" ::: "memory");
-        }
-        if (valid) {
-            uint4* p = reinterpret_cast<uint4*>(hashes + 32 * i);
-            p[0] = make_uint4(bswap(w[0]), bswap(w[1]), bswap(w[2]), bswap(w[3]));
-            p[1] = make_uint4(bswap(w[4]), bswap(w[5]), bswap(w[6]), bswap(w[7]));
-        }
-    }
-}
-
 }  // namespace
 
 cudaError_t launch_poh_verify(uint8_t* hashes, const uint64_t* num_hashes, uint64_t n, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    // pairs of warps while they fit one warp per sub-partition (GB300: 4 per SM)
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
                                                   cudaSuccess)
         return cudaGetLastError();
+    // Two warps per 32 chains while the pairs fit one warp per sub-partition.
+    // A lone warp is bound by its sub-partition's ALU pipe (one warp
+    // instruction every 2 cycles, ~1,330 per hash), and a batch of a few
+    // thousand chains leaves most sub-partitions idle: in the paired form
+    // (poh_batch.cu) one warp computes the message schedule into shared
+    // memory while the other runs the 64 rounds, ~840 instructions per hash
+    // on the round warp.
     const uint64_t groups = (n + 31) / 32;
-    if (!POH_NO_PAIR && 2 * groups <= 4ull * (uint64_t)sms) {
-        poh_pair_kernel<<<(unsigned)groups, 64, 0, s>>>(hashes, num_hashes, n);
-        return cudaGetLastError();
-    }
+    if (!POH_NO_PAIR && 2 * groups <= 4ull * (uint64_t)sms) return launch_poh_pair_direct(hashes, num_hashes, n, s);
     uint64_t blocks = (n + POH_THREADS - 1) / POH_THREADS;
     if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
     poh_verify_kernel<<<(unsigned)blocks, POH_THREADS, 0, s>>>(hashes, num_hashes, n, 1u);

@@ -60,14 +60,14 @@ __global__ void poh_scatter_kernel(const uint64_t* counts, uint64_t n, PohBatchS
     if (i < n) s->order[atomicAdd(&s->cursor[bucket_of(counts[i])], 1u)] = (uint32_t)i;
 }
 
-__device__ __forceinline__ void load_entry(const uint8_t* hashes, uint32_t e, uint32_t w[8]) {
+__device__ __forceinline__ void load_entry(const uint8_t* hashes, uint64_t e, uint32_t w[8]) {
     const uint4* p = reinterpret_cast<const uint4*>(hashes + 32ull * e);
     uint4 lo = p[0], hi = p[1];
     w[0] = bswap_u32(lo.x); w[1] = bswap_u32(lo.y); w[2] = bswap_u32(lo.z); w[3] = bswap_u32(lo.w);
     w[4] = bswap_u32(hi.x); w[5] = bswap_u32(hi.y); w[6] = bswap_u32(hi.z); w[7] = bswap_u32(hi.w);
 }
 
-__device__ __forceinline__ void store_entry(uint8_t* hashes, uint32_t e, const uint32_t w[8]) {
+__device__ __forceinline__ void store_entry(uint8_t* hashes, uint64_t e, const uint32_t w[8]) {
     uint4* p = reinterpret_cast<uint4*>(hashes + 32ull * e);
     p[0] = make_uint4(bswap_u32(w[0]), bswap_u32(w[1]), bswap_u32(w[2]), bswap_u32(w[3]));
     p[1] = make_uint4(bswap_u32(w[4]), bswap_u32(w[5]), bswap_u32(w[6]), bswap_u32(w[7]));
@@ -81,8 +81,8 @@ struct HashWords {
 // functions.  Compiled inline, their schedule depended on the code around
 // them: the single-warp loop ran at ~2,550 cycles per hash in a 32-thread
 // block but ~3,150 in a 128-thread one, and the paired loop ~2,570 inside
-// the queue loop against ~2,180 in poh.cu's poh_pair_kernel.  Compiled
-// alone they run the same in every kernel that calls them.
+// the queue loop against ~2,080 in a plain one-launch-per-batch kernel.
+// Compiled alone they run at ~2,540 (single) and ~1,950 (paired) cycles.
 static __device__ __noinline__ HashWords single_run(HashWords in, uint64_t r, uint32_t one) {
     const PohMul M(one);
     uint32_t w[8];
@@ -150,9 +150,10 @@ __global__ void __launch_bounds__(32 * BW) poh_persistent_kernel(uint8_t* hashes
     }
 }
 
-// Paired form: two warps per 32 lanes, as in poh.cu's poh_pair_kernel (the
-// schedule warp computes the message schedule into shared memory while the
-// round warp runs the rounds), inside the persistent longest-first loop.
+// Paired form: two warps per 32 lanes (the schedule warp computes the
+// message schedule K[t] + W[t], t = 16..63, into shared memory while the
+// round warp runs the 64 rounds: ~840 ALU instructions per hash on the round
+// warp instead of ~1,330), inside the persistent longest-first loop.
 // The round warp owns the queue: each refill round it stores finished
 // chains, loads new ones and the step count r (the smallest remaining count
 // among its busy lanes), and hands the current hash words and r to the
@@ -168,10 +169,16 @@ __shared__ uint32_t pair_hout[kMaxPairsPerBlock][8][32];  // hash words, round w
 __device__ __forceinline__ uint32_t sched_s0(uint32_t x) { return POH_ROTR(x, 7) ^ POH_ROTR(x, 18) ^ (x >> 3); }
 __device__ __forceinline__ uint32_t sched_s1(uint32_t x) { return POH_ROTR(x, 17) ^ POH_ROTR(x, 19) ^ (x >> 10); }
 
-// round warp of pair PI: r hashes of its 32 chains; a lane keeps its words
-// after its first `lim` hashes (lim = 0 for a lane with no chain)
+// Pair PI of its block (PI < 0: the pair index `pi` is a run-time value, so
+// every pair of a block runs one copy of the code; with one copy per pair
+// index the loops of a two-pair block outgrew the SM's instruction cache).
+#define PAIR_IDX (PI >= 0 ? (uint32_t)PI : pi)
+
+// round warp: r hashes of its 32 chains; a lane keeps its words after its
+// first `lim` hashes (lim = 0 for a lane with no chain)
 template <int PI>
-static __device__ __noinline__ HashWords pair_rounds(HashWords in, uint32_t lane, uint64_t r, uint64_t lim) {
+static __device__ __noinline__ HashWords pair_rounds(HashWords in, uint32_t lane, uint64_t r, uint64_t lim,
+                                                     uint32_t pi) {
     const uint32_t iv[8] = {0x6a09e667u, 0xbb67ae85u, 0x3c6ef372u, 0xa54ff53au,
                             0x510e527fu, 0x9b05688cu, 0x1f83d9abu, 0x5be0cd19u};
     uint32_t w[8];
@@ -182,11 +189,11 @@ static __device__ __noinline__ HashWords pair_rounds(HashWords in, uint32_t lane
         uint32_t a = iv[0], b = iv[1], c = iv[2], d = iv[3], e = iv[4], f = iv[5], g = iv[6], h = iv[7];
 #pragma unroll
         for (int t = 0; t < 64; t++) {
-            if (t == 16 || t == 32 || t == 48) asm volatile("bar.sync %0, 64;" ::"r"(6 * PI + t / 16) : "memory");
+            if (t == 16 || t == 32 || t == 48) asm volatile("bar.sync %0, 64;" ::"r"(6 * PAIR_IDX + t / 16) : "memory");
             uint32_t x;
             if (t < 8) x = w[t] + poh_k(t);
             else if (t < 16) x = (t == 8 ? 0x80000000u : t == 15 ? 256u : 0u) + poh_k(t);
-            else x = pair_kw[PI][t - 16][lane];
+            else x = pair_kw[PAIR_IDX][t - 16][lane];
             const uint32_t t1 = h + (POH_ROTR(e, 6) ^ POH_ROTR(e, 11) ^ POH_ROTR(e, 25)) + ((e & f) ^ (~e & g)) + x;
             const uint32_t t2 = (POH_ROTR(a, 2) ^ POH_ROTR(a, 13) ^ POH_ROTR(a, 22)) + ((a & b) | (c & (a | b)));
             h = g;
@@ -204,8 +211,8 @@ static __device__ __noinline__ HashWords pair_rounds(HashWords in, uint32_t lane
         w[4] = live ? iv[4] + e : w[4]; w[5] = live ? iv[5] + f : w[5];
         w[6] = live ? iv[6] + g : w[6]; w[7] = live ? iv[7] + h : w[7];
 #pragma unroll
-        for (int t = 0; t < 8; t++) pair_hout[PI][t][lane] = w[t];
-        asm volatile("bar.sync %0, 64;" ::"n"(6 * PI + 4) : "memory");
+        for (int t = 0; t < 8; t++) pair_hout[PAIR_IDX][t][lane] = w[t];
+        asm volatile("bar.sync %0, 64;" ::"r"(6 * PAIR_IDX + 4) : "memory");
     }
     HashWords out;
 #pragma unroll
@@ -213,10 +220,10 @@ static __device__ __noinline__ HashWords pair_rounds(HashWords in, uint32_t lane
     return out;
 }
 
-// schedule warp of pair PI: the message schedule of r hashes, each from the
-// hash words the round warp published at barrier 4 of the previous hash
+// schedule warp: the message schedule of r hashes, each from the hash words
+// the round warp published at barrier 4 of the previous hash
 template <int PI>
-static __device__ __noinline__ void pair_schedule(HashWords in, uint32_t lane, uint64_t r) {
+static __device__ __noinline__ void pair_schedule(HashWords in, uint32_t lane, uint64_t r, uint32_t pi) {
     uint32_t w[8];
 #pragma unroll
     for (int t = 0; t < 8; t++) w[t] = in.v[t];
@@ -236,23 +243,27 @@ static __device__ __noinline__ void pair_schedule(HashWords in, uint32_t lane, u
                 const int t = 16 + part * 16 + j;
                 const uint32_t x = W[t & 15] + sched_s0(W[(t - 15) & 15]) + W[(t - 7) & 15] + sched_s1(W[(t - 2) & 15]);
                 W[t & 15] = x;
-                pair_kw[PI][t - 16][lane] = x + poh_k(t);
+                pair_kw[PAIR_IDX][t - 16][lane] = x + poh_k(t);
             }
-            asm volatile("bar.sync %0, 64;" ::"r"(6 * PI + 1 + part) : "memory");
+            asm volatile("bar.sync %0, 64;" ::"r"(6 * PAIR_IDX + 1 + part) : "memory");
         }
-        asm volatile("bar.sync %0, 64;" ::"n"(6 * PI + 4) : "memory");
+        asm volatile("bar.sync %0, 64;" ::"r"(6 * PAIR_IDX + 4) : "memory");
 #pragma unroll
-        for (int t = 0; t < 8; t++) w[t] = pair_hout[PI][t][lane];
+        for (int t = 0; t < 8; t++) w[t] = pair_hout[PAIR_IDX][t][lane];
     }
 }
 
+// s == nullptr: direct mode, no queue; the pair takes entries 32g .. 32g + 31
+// once (g = its index in the grid), in the order given.
 template <int PI>
 __device__ __forceinline__ void pair_persistent(uint8_t* hashes, const uint64_t* counts, uint32_t n,
-                                                PohBatchScratch* s, uint64_t* run_len, uint32_t role) {
+                                                PohBatchScratch* s, uint64_t* run_len, uint32_t role, uint32_t pi,
+                                                uint32_t direct_first) {
     const uint32_t lane = threadIdx.x & 31u;
     HashWords w = {{0, 0, 0, 0, 0, 0, 0, 0}};
     uint64_t rem = 0;
     uint32_t cur = 0xffffffffu;
+    uint32_t direct_k = direct_first + lane;
     bool done = false;
     for (;;) {
         if (role == 0) {
@@ -264,15 +275,21 @@ __device__ __forceinline__ void pair_persistent(uint8_t* hashes, const uint64_t*
                     store_entry(hashes, cur, w.v);
                     cur = 0xffffffffu;
                 }
-                uint32_t base = 0;
-                if (lane == (uint32_t)(__ffs(mask) - 1)) base = atomicAdd(&s->next, (uint32_t)__popc(mask));
-                base = __shfl_sync(0xffffffffu, base, __ffs(mask) - 1);
+                uint32_t k;
+                if (s) {
+                    uint32_t base = 0;
+                    if (lane == (uint32_t)(__ffs(mask) - 1)) base = atomicAdd(&s->next, (uint32_t)__popc(mask));
+                    base = __shfl_sync(0xffffffffu, base, __ffs(mask) - 1);
+                    k = base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+                } else {
+                    k = direct_k;
+                    if (need) direct_k = 0xffffffffu;
+                }
                 if (need) {
-                    const uint32_t k = base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
                     if (k >= n) {
                         done = true;
                     } else {
-                        cur = s->order[k];
+                        cur = s ? s->order[k] : k;
                         load_entry(hashes, cur, w.v);
                         rem = counts[cur];
                     }
@@ -286,19 +303,19 @@ __device__ __forceinline__ void pair_persistent(uint8_t* hashes, const uint64_t*
             }
             if (r == ~0ull) r = 0;
 #pragma unroll
-            for (int t = 0; t < 8; t++) pair_hout[PI][t][lane] = w.v[t];
+            for (int t = 0; t < 8; t++) pair_hout[PAIR_IDX][t][lane] = w.v[t];
             if (lane == 0) *run_len = r;
         }
-        asm volatile("bar.sync %0, 64;" ::"n"(6 * PI + 5) : "memory");
+        asm volatile("bar.sync %0, 64;" ::"r"(6 * PAIR_IDX + 5) : "memory");
         const uint64_t r = *run_len;
         if (r == 0) break;
         if (role == 1) {
             HashWords h0;
 #pragma unroll
-            for (int t = 0; t < 8; t++) h0.v[t] = pair_hout[PI][t][lane];
-            pair_schedule<PI>(h0, lane, r);
+            for (int t = 0; t < 8; t++) h0.v[t] = pair_hout[PAIR_IDX][t][lane];
+            pair_schedule<PI>(h0, lane, r, pi);
         } else {
-            w = pair_rounds<PI>(w, lane, r, done ? 0 : r);
+            w = pair_rounds<PI>(w, lane, r, done ? 0 : r, pi);
             if (!done) rem -= r;
         }
     }
@@ -311,18 +328,28 @@ __global__ void __launch_bounds__(64 * P) poh_pair_persistent_kernel(uint8_t* ha
     static_assert(P >= 1 && P <= kMaxPairsPerBlock, "pairs per block");
     __shared__ uint64_t run_len[P];
     const uint32_t warp = threadIdx.x >> 5, pair = warp >> 1, role = warp & 1u;
-    if (pair == 0) pair_persistent<0>(hashes, counts, n, s, &run_len[0], role);
-    else if (P > 1) pair_persistent<1>(hashes, counts, n, s, &run_len[P > 1 ? 1 : 0], role);
+    const uint32_t first = (blockIdx.x * P + pair) * 32u;   // direct mode only
+    if (P == 1) pair_persistent<0>(hashes, counts, n, s, &run_len[0], role, 0, first);
+    else pair_persistent<-1>(hashes, counts, n, s, &run_len[pair], role, pair, first);
 }
 
 }  // namespace
 
 size_t poh_batch_workspace_size(uint64_t n) { return sizeof(PohBatchScratch) + 4ull * (n ? n : 1); }
 
+cudaError_t launch_poh_pair_direct(uint8_t* hashes, const uint64_t* counts, uint64_t n, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    if (n > 0xffffffe0ull) return cudaErrorInvalidValue;   // 32 * groups must fit 32 bits
+    const uint64_t groups = (n + 31) / 32;
+    poh_pair_persistent_kernel<1><<<(unsigned)groups, 64, 0, s>>>(hashes, counts, (uint32_t)n, nullptr);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_poh_batch(uint8_t* hashes, const uint64_t* counts, uint64_t n, void* workspace,
                              int warps, cudaStream_t s, int form) {
     if (n == 0) return cudaSuccess;
     if (n > 0xffffffffull) return cudaErrorInvalidValue;
+    if (form == kPohPairDirect) return launch_poh_pair_direct(hashes, counts, n, s);
     PohBatchScratch* sc = static_cast<PohBatchScratch*>(workspace);
     cudaError_t e = cudaMemsetAsync(sc, 0, sizeof(PohBatchScratch), s);
     if (e != cudaSuccess) return e;

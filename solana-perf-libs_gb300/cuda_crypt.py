@@ -249,11 +249,11 @@ class CudaCrypt:
         if rc != 0:
             raise RuntimeError(f"gb300_poh_verify_batch_device: cudaError {rc}")
 
-    POH_SINGLE, POH_PACKED_SINGLE, POH_PAIR, POH_PACKED_PAIR = 0, 1, 2, 3
+    POH_SINGLE, POH_PACKED_SINGLE, POH_PAIR, POH_PACKED_PAIR, POH_PAIR_DIRECT = 0, 1, 2, 3, 4
 
     def poh_verify_batch_shape(self, hashes, num_hashes, workspace, warps, form, stream=0) -> None:
         """Device PoH batch with a forced persistent launch shape (diagnostic);
-        form: POH_SINGLE, POH_PACKED_SINGLE, POH_PAIR or POH_PACKED_PAIR."""
+        form: POH_SINGLE, POH_PACKED_SINGLE, POH_PAIR, POH_PACKED_PAIR or POH_PAIR_DIRECT."""
         rc = self.lib.gb300_poh_verify_batch_shape(hashes.data_ptr(), num_hashes.data_ptr(), num_hashes.numel(),
                                                    workspace.data_ptr(), workspace.numel() * workspace.element_size(),
                                                    warps, form, stream)

@@ -127,7 +127,7 @@ def test_tuning_report(lib):
 
 
 @pytest.mark.parametrize("form,warps_per_sm", [(0, 4), (0, 8), (0, 1), (1, 4), (2, 4), (2, 8), (2, 2),
-                                               (3, 4), (3, 2)])
+                                               (3, 4), (3, 2), (4, 4)])
 def test_poh_batch_every_launch_shape(lib, oracle, form, warps_per_sm):
     """Single, packed, paired and packed-paired persistent forms, at several
     residencies (odd pair counts included), give the oracle's chains (ragged
@@ -146,7 +146,7 @@ def test_poh_batch_every_launch_shape(lib, oracle, form, warps_per_sm):
     assert np.array_equal(dh.cpu().numpy(), exp)
 
 
-@pytest.mark.parametrize("form", [0, 1, 2, 3])
+@pytest.mark.parametrize("form", [0, 1, 2, 3, 4])
 def test_poh_batch_forms_few_chains(lib, oracle, form):
     """Fewer chains than one warp (a partly empty pair and block)."""
     torch = pytest.importorskip("torch")
@@ -165,6 +165,6 @@ def test_poh_batch_shape_rejects_bad_shapes(lib):
     dh = torch.zeros((4, 32), dtype=torch.uint8, device="cuda")
     dc = torch.ones(4, dtype=torch.int64, device="cuda")
     ws = torch.empty(lib.poh_batch_workspace_size(4), dtype=torch.uint8, device="cuda")
-    for warps, form in ((0, 0), (64, 4), (64, -1), (10 ** 6, 0)):
+    for warps, form in ((0, 0), (64, 5), (64, -1), (10 ** 6, 0)):
         with pytest.raises(RuntimeError):
             lib.poh_verify_batch_shape(dh, dc, ws, warps, form)
