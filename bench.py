@@ -438,7 +438,7 @@ def _pct(xs, q):
 
 
 def bench_serving(lib, levels=(0.1, 0.25, 0.5, 0.8, 1.0, 1.2), duration_s=1.0, max_requests=2500,
-                  plain_requests=120):
+                  plain_requests=120, burst_n=1000):
     """Open-loop Poisson arrivals of a request mix (80% verify batches of the
     ragged-batch size/message/adversarial distributions, 15% PoH batches of
     64 entries with num_hashes log-uniform in 1..1e6, 5% sign batches of 128
@@ -495,7 +495,7 @@ def bench_serving(lib, levels=(0.1, 0.25, 0.5, 0.8, 1.0, 1.2), duration_s=1.0, m
     ok_all = True
     try:
         # peak: a burst of the mix, time until its signature requests are done
-        burst = draw(200)
+        burst = draw(burst_n)
         t0 = time.perf_counter()
         subs = [(kind, k) + tuple(submit(srv, kind, k)) for kind, k in burst]
         last_sig = t0
@@ -544,6 +544,12 @@ def bench_serving(lib, levels=(0.1, 0.25, 0.5, 0.8, 1.0, 1.2), duration_s=1.0, m
         stats = srv.stats()
     finally:
         srv.close()
+    if plain_requests <= 0:
+        for sp in vpool + spool:
+            for b in sp.batches:
+                lib.host_unregister(b)
+        return {"peak_requests_per_s": peak_rps, "peak_sig_items_per_s": peak_items, "levels": rows,
+                "results_identical_alone_and_in_mix": bool(ok_all), "server_stats": stats}
     # the plain per-request calls at 80% of the served peak, 4 caller threads
     lam = 0.8 * peak_rps
     n = min(plain_requests, max(30, int(lam * duration_s)))

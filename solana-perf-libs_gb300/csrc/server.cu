@@ -81,6 +81,7 @@ struct gb300_server {
     CryptDeviceInfo info{};
     uint64_t cap = 0, in_use = 0;
     uint32_t max_items = 0;
+    int poh_form = kPohPackedSingle, poh_warps = 0;   // shape of the PoH launches
     std::vector<Slot> sig_slots, poh_slots;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
@@ -204,11 +205,8 @@ cudaError_t launch_pohs(gb300_server* sv, Slot& S) {
     }
     uint8_t* d = static_cast<uint8_t*>(S.d_data.p);
     if ((e = cudaMemcpyAsync(d, st, hb + cb, cudaMemcpyHostToDevice, S.stream)) != cudaSuccess) return e;
-    // PoH warps packed four to a block (two schedule + round pairs): whole
-    // SMs' sub-partitions, not one sub-partition on every SM, so signature
-    // launches keep the other SMs
-    if ((e = launch_poh_batch(d, reinterpret_cast<const uint64_t*>(d + hb), n, S.d_scratch.p, sv->info.poh_warps,
-                              S.stream, kPohPackedPair)) != cudaSuccess)
+    if ((e = launch_poh_batch(d, reinterpret_cast<const uint64_t*>(d + hb), n, S.d_scratch.p, sv->poh_warps,
+                              S.stream, sv->poh_form)) != cudaSuccess)
         return e;
     if ((e = cudaMemcpyAsync(st, d, hb, cudaMemcpyDeviceToHost, S.stream)) != cudaSuccess) return e;
     return cudaEventRecord(S.done, S.stream);
@@ -366,6 +364,23 @@ gb300_server* gb300_server_create(const gb300_server_config* cfg) {
     if (!crypt_device_info(dev, &sv->info)) {
         delete sv;
         return nullptr;
+    }
+    // PoH launches: paired warps, one pair per SM at most (2 x SMs warps).
+    // Measured on GB300 under the served request mix, against independent
+    // warps packed four to a block and against a pair on every other
+    // sub-partition: the same signature peak (~8,950 requests/s) as the
+    // packed warps with PoH latency p50 1.31 s instead of 1.86 s; two pairs
+    // per SM cut the signature peak to ~7,300.  GB300_CRYPT_SERVER_POH_FORM
+    // (a PohBatchForm) and GB300_CRYPT_SERVER_POH_WARPS override the shape.
+    sv->poh_form = kPohPair;
+    sv->poh_warps = sv->info.poh_warps / 2 > 2 ? sv->info.poh_warps / 2 : 2;
+    if (const char* v = getenv("GB300_CRYPT_SERVER_POH_FORM")) {
+        const int f = atoi(v);
+        if (f >= kPohSingle && f <= kPohPackedPair) sv->poh_form = f;
+    }
+    if (const char* v = getenv("GB300_CRYPT_SERVER_POH_WARPS")) {
+        const int w = atoi(v);
+        if (w > 0 && w <= 64 * sv->info.sms) sv->poh_warps = w;
     }
     sv->cap = cfg && cfg->device_memory_cap ? cfg->device_memory_cap : (8ull << 30);
     sv->max_items = cfg && cfg->max_items_per_launch ? cfg->max_items_per_launch : 65536u;
