@@ -176,9 +176,20 @@ __device__ __forceinline__ uint32_t sched_s1(uint32_t x) { return POH_ROTR(x, 17
 
 // round warp: r hashes of its 32 chains; a lane keeps its words after its
 // first `lim` hashes (lim = 0 for a lane with no chain)
+// Round additions issued on the multiply pipe as x * one + y (one == 1 at
+// run time, so the compiler keeps the multiply-add): bit 2 h + K[t] + W[t],
+// bit 0 e' = d + t1, bit 1 t2 = S0 + Maj, bit 3 a' = t1 + t2.  The round
+// warp is bound by its ALU pipe; h + K + W is off the critical path, and
+// moving it gained 2.0 % on GB300 (1,898 -> 1,860 cycles per hash).  The
+// other additions are on the e / a dependency chains, where the multiply
+// pipe's longer latency cost 3-20 %.
+#ifndef POH_PAIR_MADD
+#define POH_PAIR_MADD 4
+#endif
+
 template <int PI>
 static __device__ __noinline__ HashWords pair_rounds(HashWords in, uint32_t lane, uint64_t r, uint64_t lim,
-                                                     uint32_t pi) {
+                                                     uint32_t pi, uint32_t one) {
     const uint32_t iv[8] = {0x6a09e667u, 0xbb67ae85u, 0x3c6ef372u, 0xa54ff53au,
                             0x510e527fu, 0x9b05688cu, 0x1f83d9abu, 0x5be0cd19u};
     uint32_t w[8];
@@ -194,16 +205,21 @@ static __device__ __noinline__ HashWords pair_rounds(HashWords in, uint32_t lane
             if (t < 8) x = w[t] + poh_k(t);
             else if (t < 16) x = (t == 8 ? 0x80000000u : t == 15 ? 256u : 0u) + poh_k(t);
             else x = pair_kw[PAIR_IDX][t - 16][lane];
-            const uint32_t t1 = h + (POH_ROTR(e, 6) ^ POH_ROTR(e, 11) ^ POH_ROTR(e, 25)) + ((e & f) ^ (~e & g)) + x;
-            const uint32_t t2 = (POH_ROTR(a, 2) ^ POH_ROTR(a, 13) ^ POH_ROTR(a, 22)) + ((a & b) | (c & (a | b)));
+            const uint32_t S1 = POH_ROTR(e, 6) ^ POH_ROTR(e, 11) ^ POH_ROTR(e, 25);
+            const uint32_t ch = (e & f) ^ (~e & g);
+            const uint32_t S0 = POH_ROTR(a, 2) ^ POH_ROTR(a, 13) ^ POH_ROTR(a, 22);
+            const uint32_t maj = (a & b) | (c & (a | b));
+            const uint32_t hx = (POH_PAIR_MADD & 4) ? add_mul(h, x, one) : h + x;
+            const uint32_t t1 = hx + S1 + ch;
+            const uint32_t t2 = (POH_PAIR_MADD & 2) ? add_mul(S0, maj, one) : S0 + maj;
             h = g;
             g = f;
             f = e;
-            e = d + t1;
+            e = (POH_PAIR_MADD & 1) ? add_mul(d, t1, one) : d + t1;
             d = c;
             c = b;
             b = a;
-            a = t1 + t2;
+            a = (POH_PAIR_MADD & 8) ? add_mul(t1, t2, one) : t1 + t2;
         }
         const bool live = k < lim;
         w[0] = live ? iv[0] + a : w[0]; w[1] = live ? iv[1] + b : w[1];
@@ -258,7 +274,7 @@ static __device__ __noinline__ void pair_schedule(HashWords in, uint32_t lane, u
 template <int PI>
 __device__ __forceinline__ void pair_persistent(uint8_t* hashes, const uint64_t* counts, uint32_t n,
                                                 PohBatchScratch* s, uint64_t* run_len, uint32_t role, uint32_t pi,
-                                                uint32_t direct_first) {
+                                                uint32_t direct_first, uint32_t one) {
     const uint32_t lane = threadIdx.x & 31u;
     HashWords w = {{0, 0, 0, 0, 0, 0, 0, 0}};
     uint64_t rem = 0;
@@ -315,7 +331,7 @@ __device__ __forceinline__ void pair_persistent(uint8_t* hashes, const uint64_t*
             for (int t = 0; t < 8; t++) h0.v[t] = pair_hout[PAIR_IDX][t][lane];
             pair_schedule<PI>(h0, lane, r, pi);
         } else {
-            w = pair_rounds<PI>(w, lane, r, done ? 0 : r, pi);
+            w = pair_rounds<PI>(w, lane, r, done ? 0 : r, pi, one);
             if (!done) rem -= r;
         }
     }
@@ -324,13 +340,13 @@ __device__ __forceinline__ void pair_persistent(uint8_t* hashes, const uint64_t*
 // P pairs per block: warps 2p (rounds, queue) and 2p + 1 (schedule)
 template <int P>
 __global__ void __launch_bounds__(64 * P) poh_pair_persistent_kernel(uint8_t* hashes, const uint64_t* counts,
-                                                                     uint32_t n, PohBatchScratch* s) {
+                                                                     uint32_t n, PohBatchScratch* s, uint32_t one) {
     static_assert(P >= 1 && P <= kMaxPairsPerBlock, "pairs per block");
     __shared__ uint64_t run_len[P];
     const uint32_t warp = threadIdx.x >> 5, pair = warp >> 1, role = warp & 1u;
     const uint32_t first = (blockIdx.x * P + pair) * 32u;   // direct mode only
-    if (P == 1) pair_persistent<0>(hashes, counts, n, s, &run_len[0], role, 0, first);
-    else pair_persistent<-1>(hashes, counts, n, s, &run_len[pair], role, pair, first);
+    if (P == 1) pair_persistent<0>(hashes, counts, n, s, &run_len[0], role, 0, first, one);
+    else pair_persistent<-1>(hashes, counts, n, s, &run_len[pair], role, pair, first, one);
 }
 
 }  // namespace
@@ -341,7 +357,7 @@ cudaError_t launch_poh_pair_direct(uint8_t* hashes, const uint64_t* counts, uint
     if (n == 0) return cudaSuccess;
     if (n > 0xffffffe0ull) return cudaErrorInvalidValue;   // 32 * groups must fit 32 bits
     const uint64_t groups = (n + 31) / 32;
-    poh_pair_persistent_kernel<1><<<(unsigned)groups, 64, 0, s>>>(hashes, counts, (uint32_t)n, nullptr);
+    poh_pair_persistent_kernel<1><<<(unsigned)groups, 64, 0, s>>>(hashes, counts, (uint32_t)n, nullptr, 1u);
     return cudaGetLastError();
 }
 
@@ -367,10 +383,11 @@ cudaError_t launch_poh_batch(uint8_t* hashes, const uint64_t* counts, uint64_t n
             poh_persistent_kernel<4><<<(unsigned)((nwarps + 3) / 4), 128, 0, s>>>(hashes, counts, (uint32_t)n, sc, 1u);
             break;
         case kPohPair:
-            poh_pair_persistent_kernel<1><<<(unsigned)pairs, 64, 0, s>>>(hashes, counts, (uint32_t)n, sc);
+            poh_pair_persistent_kernel<1><<<(unsigned)pairs, 64, 0, s>>>(hashes, counts, (uint32_t)n, sc, 1u);
             break;
         case kPohPackedPair:
-            poh_pair_persistent_kernel<2><<<(unsigned)((pairs + 1) / 2), 128, 0, s>>>(hashes, counts, (uint32_t)n, sc);
+            poh_pair_persistent_kernel<2><<<(unsigned)((pairs + 1) / 2), 128, 0, s>>>(hashes, counts, (uint32_t)n, sc,
+                                                                                    1u);
             break;
         default:
             poh_persistent_kernel<1><<<(unsigned)nwarps, 32, 0, s>>>(hashes, counts, (uint32_t)n, sc, 1u);
