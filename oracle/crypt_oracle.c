@@ -966,3 +966,74 @@ void oracle_create_keypairs(const u8 *seeds, u8 *pk, u8 *sk, size_t n, int nthre
     j.n = n;
     run_jobs(j, nthreads);
 }
+
+/* ---- Solana wire-format packets ------------------------------------------
+ * Not part of the reference: the reference's caller (solana-perf, README.md:
+ * 27-31) parses transactions on the host and passes the four offset arrays
+ * to ed25519_verify_many.  This restates that parse from the published
+ * transaction layout, as the checker of the library's on-device parse;
+ * there is no reference code or fixture for it, so its parity is unpinned.
+ *
+ * Packet p occupies data[p * stride, p * stride + lens[p]); lens[p] > stride
+ * makes the packet malformed.  A transaction is
+ *   compact-u16 signature count n (n >= 1), n signatures of 64 bytes,
+ *   the message: an optional version byte (top bit set; only version 0 is
+ *   accepted), a 3-byte header whose first byte is the number of required
+ *   signatures (must equal n), a compact-u16 account-key count k (k >= n)
+ *   and k keys of 32 bytes, then the rest of the message.
+ * Signature i verifies with key i over the message bytes, from the message
+ * start to the end of the packet.  compact-u16: 7-bit little-endian groups,
+ * top bit = more bytes follow, at most 3 bytes, no redundant zero group,
+ * value <= 0xffff.  A malformed packet has count 0. */
+static int cu16_read(const u8 *p, u32 len, u32 *pos, u32 *val) {
+    u32 v = 0;
+    for (u32 i = 0; i < 3; i++) {
+        if (*pos + i >= len) return 0;
+        const u32 b = p[*pos + i];
+        v |= (b & 0x7fu) << (7 * i);
+        if (!(b & 0x80u)) {
+            if (i > 0 && b == 0) return 0;       /* redundant zero group */
+            if (i == 2 && b > 3) return 0;       /* above 0xffff */
+            *pos += i + 1;
+            *val = v;
+            return 1;
+        }
+    }
+    return 0;                                    /* a fourth byte */
+}
+
+/* count of signatures (0: malformed); offsets relative to the packet start */
+u32 oracle_parse_packet(const u8 *p, u32 len, u32 *sig_off, u32 *key_off, u32 *msg_off) {
+    u32 pos = 0, n = 0, k = 0;
+    if (!cu16_read(p, len, &pos, &n) || n == 0) return 0;
+    *sig_off = pos;
+    if ((u64)pos + 64ull * n > len) return 0;
+    pos += 64 * n;
+    *msg_off = pos;
+    if (pos >= len) return 0;
+    if (p[pos] & 0x80u) {
+        if ((p[pos] & 0x7fu) != 0) return 0;
+        pos++;
+    }
+    if ((u64)pos + 3 > len) return 0;
+    if (p[pos] != n) return 0;
+    pos += 3;
+    if (!cu16_read(p, len, &pos, &k) || k < n) return 0;
+    *key_off = pos;
+    if ((u64)pos + 32ull * k > len) return 0;
+    return n;
+}
+
+void oracle_parse_packets(const u8 *data, u64 stride, u32 n, const u32 *lens, u32 *counts, u32 *sig_off,
+                          u32 *key_off, u32 *msg_off, u32 *msg_len) {
+    for (u32 p = 0; p < n; p++) {
+        const u64 base = (u64)p * stride;
+        u32 so = 0, ko = 0, mo = 0;
+        const u32 c = lens[p] > stride ? 0 : oracle_parse_packet(data + base, lens[p], &so, &ko, &mo);
+        counts[p] = c;
+        sig_off[p] = c ? (u32)(base + so) : 0;
+        key_off[p] = c ? (u32)(base + ko) : 0;
+        msg_off[p] = c ? (u32)(base + mo) : 0;
+        msg_len[p] = c ? lens[p] - mo : 0;
+    }
+}

@@ -83,6 +83,8 @@ class Oracle(_Lib):
         L.oracle_sign_many.argtypes = [_u8p, ctypes.c_uint32, _u32p, _u32p, _u32p, _u32p, _u8p, ctypes.c_int]
         L.oracle_poh_verify_many.argtypes = [_u8p, _u64p, ctypes.c_size_t, ctypes.c_int]
         L.oracle_create_keypairs.argtypes = [_u8p, _u8p, _u8p, ctypes.c_size_t, ctypes.c_int]
+        L.oracle_parse_packets.argtypes = [_u8p, ctypes.c_uint64, ctypes.c_uint32, _u32p] + [_u32p] * 5
+        L.oracle_parse_packets.restype = None
 
     # ---- single items -----------------------------------------------------
     def create_keypair(self, seed: bytes):
@@ -191,6 +193,40 @@ class Oracle(_Lib):
         self.lib.oracle_sign_many(_ptr(packets, _u8p), n, *[_ptr(a, _u32p) for a in arrs],
                                   _ptr(out, _u8p), nthreads)
         return out
+
+    def parse_packets(self, data: np.ndarray, stride: int, lens):
+        """Per packet: (counts, signature, key and message offsets, message
+        lengths), offsets absolute in `data` (oracle_parse_packets)."""
+        lens = np.ascontiguousarray(lens, dtype=np.uint32)
+        n = len(lens)
+        data = np.ascontiguousarray(data, dtype=np.uint8).ravel()
+        outs = [np.zeros(n, dtype=np.uint32) for _ in range(5)]
+        self.lib.oracle_parse_packets(_ptr(data, _u8p), ctypes.c_uint64(stride), n, _ptr(lens, _u32p),
+                                      *[_ptr(a, _u32p) for a in outs])
+        return tuple(outs)
+
+    def wire_offsets(self, data: np.ndarray, stride: int, lens):
+        """The reference's four per-signature arrays for a packet batch, plus
+        the per-packet counts: (counts, message_lens, public_key_offsets,
+        signature_offsets, message_start_offsets)."""
+        counts, so, ko, mo, ml = self.parse_packets(data, stride, lens)
+        total = int(counts.sum())
+        pkt = np.repeat(np.arange(len(counts)), counts)
+        first = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.int64)
+        idx = np.arange(total) - first[pkt]
+        return (counts, ml[pkt].astype(np.uint32), (ko[pkt] + 32 * idx).astype(np.uint32),
+                (so[pkt] + 64 * idx).astype(np.uint32), mo[pkt].astype(np.uint32))
+
+    def verify_wire_packets(self, data: np.ndarray, stride: int, lens, nthreads: int = 0):
+        """(per-packet verdicts, per-signature verdicts, counts): a packet
+        passes when it parses and every one of its signatures verifies."""
+        counts, ml, ko, so, mo = self.wire_offsets(data, stride, lens)
+        sig = self.verify_many(np.ascontiguousarray(data, dtype=np.uint8).ravel(), ml, ko, so, mo,
+                               nthreads or os.cpu_count() or 1)
+        pkt = np.repeat(np.arange(len(counts)), counts)
+        bad = np.zeros(len(counts), dtype=np.int64)
+        np.add.at(bad, pkt, (sig == 0).astype(np.int64))
+        return ((counts > 0) & (bad == 0)).astype(np.uint8), sig, counts
 
     def poh_verify_many(self, hashes: np.ndarray, num_hashes, nthreads: int = 1) -> np.ndarray:
         """Returns the final hashes (the input array is not modified)."""

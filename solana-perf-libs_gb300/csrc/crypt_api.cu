@@ -26,6 +26,7 @@
 
 #include "ed25519.h"
 #include "poh_verify.h"
+#include "gb300_packets.h"
 #include "kernels.h"
 #include "tables.cuh"
 #include "host_buffers.h"
@@ -69,10 +70,11 @@ struct Queue {
     cudaStream_t stream = nullptr;
     DevBuf d_data, d_index, d_out, d_scratch;
     HostBuf h_stage, h_out;
-    GraphCache g_poh, g_sig;
+    GraphCache g_poh, g_sig, g_pkt;
     void release_buffers() {
         g_poh.reset();
         g_sig.reset();
+        g_pkt.reset();
         d_data.release();
         d_index.release();
         d_out.release();
@@ -973,6 +975,114 @@ int gb300_ed25519_batch(const gb300_sig_job* jobs, uint32_t num_jobs) {
         cudaGetLastError();
         for (uint32_t j = 0; j < num_jobs; j++)
             if (jobs[j].out && jobs[j].num) memset(jobs[j].out, 0, jobs[j].kind == 0 ? jobs[j].num : 64ull * jobs[j].num);
+    }
+    return t_last_error = (int)e;
+}
+
+// ---------------------------------------------------------------------------
+// Solana wire-format packet batches (gb300_packets.h; kernels in packets.cu).
+
+size_t gb300_packets_workspace_size(uint32_t num_packets, uint64_t stride) {
+    return packets_workspace_size(num_packets, stride);
+}
+
+uint64_t gb300_packets_signature_capacity(uint32_t num_packets, uint64_t stride) {
+    return packets_signature_capacity(num_packets, stride);
+}
+
+int gb300_packets_extract_offsets_device(const uint8_t* packets, uint64_t stride, uint32_t num_packets,
+                                         const uint32_t* packet_lens, void* workspace, size_t workspace_bytes,
+                                         uint32_t* message_lens, uint32_t* public_key_offsets,
+                                         uint32_t* signature_offsets, uint32_t* message_start_offsets,
+                                         uint32_t* sig_counts, uint32_t* total_signatures, void* stream) {
+    return (int)launch_packets_extract(packets, stride, num_packets, packet_lens, workspace, workspace_bytes,
+                                       message_lens, public_key_offsets, signature_offsets, message_start_offsets,
+                                       sig_counts, total_signatures, static_cast<cudaStream_t>(stream));
+}
+
+int gb300_ed25519_verify_packets_device(const uint8_t* packets, uint64_t stride, uint32_t num_packets,
+                                        const uint32_t* packet_lens, void* workspace, size_t workspace_bytes,
+                                        uint8_t* packet_out, uint32_t* sig_counts, void* stream) {
+    if (num_packets == 0) return 0;
+    Device* D = current_device();
+    if (!D) return (int)cudaErrorNoDevice;
+    const Tuning& T = tuning_for(*D);
+    return (int)launch_packets_verify(packets, stride, num_packets, packet_lens, workspace, workspace_bytes,
+                                      packet_out, sig_counts, D->tables, T.sig_threads, T.sig_blocks_per_sm,
+                                      D->sms, static_cast<cudaStream_t>(stream));
+}
+
+int gb300_ed25519_verify_packets(const gpu_Elems* elems, uint32_t num_elems, uint32_t stride,
+                                 const uint32_t* packet_lens, uint8_t* packet_out, uint32_t* sig_counts) {
+    uint64_t np = 0;
+    if (num_elems && !elems) return t_last_error = (int)cudaErrorInvalidValue;
+    for (uint32_t i = 0; i < num_elems; i++) np += elems[i].num;
+    if (np == 0) return 0;
+    if (!packet_lens || !packet_out || stride == 0) return t_last_error = (int)cudaErrorInvalidValue;
+    const uint64_t total = np * stride;
+    if (np > 0xffffffffull || total > 0xffffffffull) {
+        memset(packet_out, 0, np);
+        if (sig_counts) memset(sig_counts, 0, 4 * np);
+        return t_last_error = (int)cudaErrorInvalidValue;
+    }
+    const uint32_t n = (uint32_t)np;
+    Lease L;
+    if (!acquire(L)) {
+        memset(packet_out, 0, np);
+        if (sig_counts) memset(sig_counts, 0, 4 * np);
+        return t_last_error = (int)cudaErrorNoDevice;
+    }
+    const Tuning& T = tuning_for(*L.dev);
+    Queue& Q = *L.q;
+    cudaStream_t s = Q.stream;
+    auto run = [&]() -> cudaError_t {
+        bool all_locked = true;
+        for (uint32_t i = 0; i < num_elems && all_locked; i++)
+            if (elems[i].num) all_locked = is_page_locked(elems[i].elems);
+        const size_t lens_bytes = 4ull * n;
+        const size_t pk_off = round_up(lens_bytes, 256);
+        const size_t out_off = round_up(n, 256);               // d_out: verdicts, then counts
+        const size_t out_bytes = out_off + 4ull * n;
+        const size_t ws_bytes = packets_workspace_size(n, stride);
+        TRY(Q.d_data.ensure(round_up(total, 256) + lens_bytes, s));
+        TRY(Q.d_scratch.ensure(ws_bytes, s));
+        TRY(Q.d_out.ensure(out_bytes, s));
+        TRY(Q.h_stage.ensure(pk_off + (all_locked ? 0 : total)));
+        TRY(Q.h_out.ensure(out_bytes));
+        uint8_t* dpk = static_cast<uint8_t*>(Q.d_data.p);
+        uint32_t* dlens = reinterpret_cast<uint32_t*>(dpk + round_up(total, 256));
+        memcpy(Q.h_stage.p, packet_lens, lens_bytes);
+        TRY(cudaMemcpyAsync(dlens, Q.h_stage.p, lens_bytes, cudaMemcpyHostToDevice, s));
+        uint64_t cur = 0;
+        uint8_t* img = static_cast<uint8_t*>(Q.h_stage.p) + pk_off;
+        for (uint32_t i = 0; i < num_elems; i++) {
+            const uint64_t b = (uint64_t)elems[i].num * stride;
+            if (!b) continue;
+            if (all_locked) TRY(cudaMemcpyAsync(dpk + cur, elems[i].elems, b, cudaMemcpyHostToDevice, s));
+            else memcpy(img + cur, elems[i].elems, b);
+            cur += b;
+        }
+        if (!all_locked) TRY(cudaMemcpyAsync(dpk, img, total, cudaMemcpyHostToDevice, s));
+        uint8_t* dout = static_cast<uint8_t*>(Q.d_out.p);
+        uint32_t* dcnt = reinterpret_cast<uint32_t*>(dout + out_off);
+        std::vector<uint64_t> key = {1, n, stride, (uint64_t)(uintptr_t)dpk, (uint64_t)(uintptr_t)Q.d_scratch.p,
+                                     (uint64_t)(uintptr_t)dout, (uint64_t)T.sig_threads};
+        TRY(run_graph(Q.g_pkt, key, s, [&](cudaStream_t cs) {
+            return launch_packets_verify(dpk, stride, n, dlens, Q.d_scratch.p, ws_bytes, dout, dcnt, L.dev->tables,
+                                         T.sig_threads, T.sig_blocks_per_sm, L.dev->sms, cs);
+        }));
+        TRY(cudaMemcpyAsync(Q.h_out.p, dout, out_bytes, cudaMemcpyDeviceToHost, s));
+        TRY(cudaStreamSynchronize(s));
+        memcpy(packet_out, Q.h_out.p, n);
+        if (sig_counts) memcpy(sig_counts, static_cast<uint8_t*>(Q.h_out.p) + out_off, 4ull * n);
+        return cudaSuccess;
+    };
+    cudaError_t e = run();
+    if (e != cudaSuccess) {
+        fprintf(stderr, "libcuda-crypt: gb300_ed25519_verify_packets failed: %s\n", cudaGetErrorString(e));
+        cudaGetLastError();
+        memset(packet_out, 0, np);
+        if (sig_counts) memset(sig_counts, 0, 4 * np);
     }
     return t_last_error = (int)e;
 }

@@ -67,8 +67,32 @@ struct SigWork {
     uint32_t sign_base;      // first sign item's queue position (multiple of 32)
     uint32_t total_chunks;   // chunks of 32 items
     uint32_t* next;          // queue head, device word (reset by the launch)
+    // Verify-only launches whose item count is produced on the device: the
+    // kernel verifies *count_dev items (v.n and total_chunks are then the
+    // capacity, used only to size the grid).
+    const uint32_t* count_dev = nullptr;
 };
 cudaError_t launch_sig_batch(const SigWork& w, int threads, int blocks_per_sm, int sms, cudaStream_t s);
+
+// Solana wire-format packet batches (packets.cu): `n` packet slots `stride`
+// bytes apart in one device buffer, lens[i] bytes of transaction data in
+// slot i.  The workspace (packets_workspace_size bytes, 256-byte aligned)
+// holds the parse results and up to packets_signature_capacity signatures.
+size_t packets_workspace_size(uint32_t n, uint64_t stride);
+uint64_t packets_signature_capacity(uint32_t n, uint64_t stride);
+// The reference's four per-signature arrays (capacity entries each),
+// per-packet signature counts (nullable) and the total (device word,
+// nullable), all produced on the device.
+cudaError_t launch_packets_extract(const uint8_t* data, uint64_t stride, uint32_t n, const uint32_t* lens, void* ws,
+                                   size_t ws_bytes, uint32_t* message_lens, uint32_t* key_offsets,
+                                   uint32_t* sig_offsets, uint32_t* msg_offsets, uint32_t* counts_out,
+                                   uint32_t* total_out, cudaStream_t s);
+// Parse, verify every signature, packet_out[i] = 1 iff packet i parsed and
+// all its signatures verified; counts_out (nullable) = signatures per packet.
+cudaError_t launch_packets_verify(const uint8_t* data, uint64_t stride, uint32_t n, const uint32_t* lens, void* ws,
+                                  size_t ws_bytes, uint8_t* packet_out, uint32_t* counts_out,
+                                  const CurveTables* tables, int sig_threads, int sig_blocks_per_sm, int sms,
+                                  cudaStream_t s);
 
 // Per-device state the served loop (server.cu) needs from the pool
 // (crypt_api.cu): device tables and the autotuner's launch shapes.

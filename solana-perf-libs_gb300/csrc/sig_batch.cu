@@ -28,15 +28,17 @@ __global__ void __launch_bounds__(T) sig_persistent_kernel(SigWork w) {
     for (int k = threadIdx.x; k < VB_WORDS * VB_ENTRIES; k += blockDim.x) sVB[k] = w.v.tables->vb[k];
     __syncthreads();
     const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t vn = w.count_dev ? *w.count_dev : w.v.n;
+    const uint32_t chunks = w.count_dev ? (vn + 31u) / 32u : w.total_chunks;
     for (;;) {
         uint32_t c = 0;
         if (lane == 0) c = atomicAdd(w.next, 1u);
         c = __shfl_sync(0xffffffffu, c, 0);
-        if (c >= w.total_chunks) break;
+        if (c >= chunks) break;
         const uint32_t start = c * 32u;
         if (start < w.sign_base) {
             const uint32_t i = start + lane;
-            if (i < w.v.n) w.v.out[i] = verify_one(w.v, sVB, i) ? 1 : 0;
+            if (i < vn) w.v.out[i] = verify_one(w.v, sVB, i) ? 1 : 0;
         } else {
             const uint32_t i = start - w.sign_base + lane;
             if (i < w.s.n) sign_one(w.s, i);

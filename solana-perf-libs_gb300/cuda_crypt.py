@@ -126,6 +126,21 @@ class CudaCrypt:
                                                    ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int,
                                                    ctypes.c_void_p]
         L.gb300_poh_verify_batch_shape.restype = ctypes.c_int
+        L.gb300_packets_workspace_size.argtypes = [ctypes.c_uint32, ctypes.c_uint64]
+        L.gb300_packets_workspace_size.restype = ctypes.c_size_t
+        L.gb300_packets_signature_capacity.argtypes = [ctypes.c_uint32, ctypes.c_uint64]
+        L.gb300_packets_signature_capacity.restype = ctypes.c_uint64
+        L.gb300_packets_extract_offsets_device.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
+                                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t] + \
+            [ctypes.c_void_p] * 7
+        L.gb300_packets_extract_offsets_device.restype = ctypes.c_int
+        L.gb300_ed25519_verify_packets_device.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
+                                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.gb300_ed25519_verify_packets_device.restype = ctypes.c_int
+        L.gb300_ed25519_verify_packets.argtypes = [ctypes.POINTER(GpuElems), ctypes.c_uint32, ctypes.c_uint32,
+                                                   _u32p, _u8p, _u32p]
+        L.gb300_ed25519_verify_packets.restype = ctypes.c_int
 
     # ---- reference entry points ------------------------------------------
     def init(self) -> bool:
@@ -259,6 +274,51 @@ class CudaCrypt:
                                                    warps, form, stream)
         if rc != 0:
             raise RuntimeError(f"gb300_poh_verify_batch_shape: cudaError {rc}")
+
+    # ---- Solana wire-format packets (gb300_packets.h) ----
+    def packets_workspace_size(self, n: int, stride: int) -> int:
+        return int(self.lib.gb300_packets_workspace_size(n, stride))
+
+    def packets_signature_capacity(self, n: int, stride: int) -> int:
+        return int(self.lib.gb300_packets_signature_capacity(n, stride))
+
+    def verify_packets(self, data: np.ndarray, lens, batches: int = 1):
+        """Host form.  `data`: (n, stride) uint8 packet slots, split into
+        `batches` gpu_Elems runs; returns (packet verdicts, signatures per
+        packet)."""
+        assert data.dtype == np.uint8 and data.ndim == 2 and data.flags["C_CONTIGUOUS"]
+        n, stride = data.shape
+        lens = np.ascontiguousarray(lens, dtype=np.uint32)
+        cuts = np.linspace(0, n, batches + 1).astype(int)
+        elems = (GpuElems * batches)()
+        for i in range(batches):
+            elems[i].elems = _p(data[cuts[i]:], _u8p) if cuts[i] < n else None
+            elems[i].num = int(cuts[i + 1] - cuts[i])
+        out = np.zeros(n, dtype=np.uint8)
+        counts = np.zeros(n, dtype=np.uint32)
+        rc = self.lib.gb300_ed25519_verify_packets(elems, batches, stride, _p(lens, _u32p), _p(out, _u8p),
+                                                   _p(counts, _u32p))
+        if rc != 0:
+            raise RuntimeError(f"gb300_ed25519_verify_packets: cudaError {rc}")
+        return out, counts
+
+    def verify_packets_device(self, data, stride, lens, workspace, out, counts=None, stream=0) -> None:
+        rc = self.lib.gb300_ed25519_verify_packets_device(
+            data.data_ptr(), stride, lens.numel(), lens.data_ptr(), workspace.data_ptr(),
+            workspace.numel() * workspace.element_size(), out.data_ptr(),
+            counts.data_ptr() if counts is not None else None, stream)
+        if rc != 0:
+            raise RuntimeError(f"gb300_ed25519_verify_packets_device: cudaError {rc}")
+
+    def extract_offsets_device(self, data, stride, lens, workspace, message_lens, key_offsets, sig_offsets,
+                               msg_offsets, counts=None, total=None, stream=0) -> None:
+        rc = self.lib.gb300_packets_extract_offsets_device(
+            data.data_ptr(), stride, lens.numel(), lens.data_ptr(), workspace.data_ptr(),
+            workspace.numel() * workspace.element_size(), message_lens.data_ptr(), key_offsets.data_ptr(),
+            sig_offsets.data_ptr(), msg_offsets.data_ptr(), counts.data_ptr() if counts is not None else None,
+            total.data_ptr() if total is not None else None, stream)
+        if rc != 0:
+            raise RuntimeError(f"gb300_packets_extract_offsets_device: cudaError {rc}")
 
     def ed25519_batch_device(self, packets, v, v_out, s, s_out, queue_word, stream=0) -> None:
         """v / s: 4 device int32 tensors (lens, pubkey, sig-or-privkey, message offsets)."""

@@ -19,6 +19,11 @@ Workloads (sizes and distributions of the reference-facing benchmark set):
                    message bit.
   poh_ragged       16384 entries, num_hashes log-uniform in 1..1e6, 3%
                    corrupted expected hashes.
+  wire_packets     Solana wire-format transactions (legacy and version-0
+                   messages, 1..4 signers, random account keys, blockhash
+                   and instructions) in fixed-stride packet slots with a
+                   per-packet data length; a fraction corrupted (flipped
+                   signature or message bit) and a fraction malformed.
 """
 from __future__ import annotations
 
@@ -208,3 +213,134 @@ def corrupt_expected(expected: np.ndarray, frac: float, seed: int):
         bit = int(rng.integers(0, 256))
         exp[i, bit // 8] ^= np.uint8(1 << (bit % 8))
     return exp, mask
+
+
+# ------------------------------------------------------- wire packets ---
+
+PACKET_DATA_SIZE = 1232        # bytes of transaction data a packet slot holds
+WIRE_STRIDE = 1280             # slot stride: data plus room for metadata
+
+MALFORMED_KINDS = ("truncated", "count_mismatch", "zero_signatures", "few_keys", "bad_version",
+                   "redundant_cu16", "len_over_stride")
+
+
+def cu16(v: int) -> bytes:
+    """compact-u16 encoding (7-bit groups, little-endian, top bit = more)."""
+    out = bytearray()
+    while True:
+        b = v & 0x7F
+        v >>= 7
+        if v:
+            out.append(b | 0x80)
+        else:
+            out.append(b)
+            return bytes(out)
+
+
+@dataclass
+class WirePackets:
+    data: np.ndarray            # (n, stride) uint8 packet slots
+    stride: int
+    lens: np.ndarray            # uint32 bytes of wire data per packet
+    kinds: list                 # per packet: "valid", "corrupt_sig", "corrupt_msg" or a MALFORMED_KINDS entry
+
+
+def _message(rng, signer_pks, versioned: bool) -> bytes:
+    nsig = len(signer_pks)
+    nkeys = nsig + int(rng.integers(0, 7))
+    keys = [bytes(pk) for pk in signer_pks] + [rng.bytes(32) for _ in range(nkeys - nsig)]
+    hdr = bytes([nsig, int(rng.integers(0, nsig)), int(rng.integers(0, nkeys - nsig + 1))])
+    body = bytearray()
+    if versioned:
+        body.append(0x80)
+    body += hdr + cu16(nkeys) + b"".join(keys) + rng.bytes(32)       # keys, recent blockhash
+    nins = int(rng.integers(1, 4))
+    body += cu16(nins)
+    for _ in range(nins):
+        nacc = int(rng.integers(0, min(nkeys, 8) + 1))
+        data = rng.bytes(int(rng.integers(0, 160)))
+        body += bytes([int(rng.integers(0, nkeys))]) + cu16(nacc) + \
+            bytes(int(x) for x in rng.integers(0, nkeys, nacc)) + cu16(len(data)) + data
+    if versioned:
+        body += cu16(0)                                               # no address-table lookups
+    return bytes(body)
+
+
+def wire_packets(keypairs, sign, n: int = 4096, corrupt_frac: float = 0.05, malformed_frac: float = 0.03,
+                 seed: int = 11, stride: int = WIRE_STRIDE) -> WirePackets:
+    """`n` packets; signatures made with `keypairs` / `sign` as elsewhere."""
+    rng = np.random.default_rng(seed)
+    nsig = rng.choice([1, 1, 1, 2, 2, 3, 4], n)
+    total = int(nsig.sum())
+    pk, sk = keypairs(rng.integers(0, 256, (total, 32), dtype=np.uint8))
+    msgs, first = [], 0
+    for p in range(n):
+        k = int(nsig[p])
+        m = _message(rng, pk[first:first + k], bool(rng.random() < 0.5))
+        while len(cu16(k)) + 64 * k + len(m) > PACKET_DATA_SIZE:
+            m = m[:PACKET_DATA_SIZE - len(cu16(k)) - 64 * k]
+        msgs.append(m)
+        first += k
+    # signing image: per signature [sk 64][pk 32][message]
+    simg, lens, pko, sko, mso, off = [], [], [], [], [], 0
+    first = 0
+    for p in range(n):
+        for j in range(int(nsig[p])):
+            s = first + j
+            simg.append(bytes(sk[s]) + bytes(pk[s]) + msgs[p])
+            sko.append(off)
+            pko.append(off + 64)
+            mso.append(off + 96)
+            lens.append(len(msgs[p]))
+            off += 96 + len(msgs[p])
+        first += int(nsig[p])
+    flat = np.frombuffer(b"".join(simg), dtype=np.uint8).copy()
+    sigs = sign(SigPackets([flat], len(flat), np.array(lens, np.uint32), np.array(pko, np.uint32),
+                           np.array(sko, np.uint32), np.array(mso, np.uint32)))
+    data = np.zeros((n, stride), dtype=np.uint8)
+    plen = np.zeros(n, dtype=np.uint32)
+    kinds = []
+    first = 0
+    u = rng.random(n)
+    for p in range(n):
+        k = int(nsig[p])
+        tx = bytearray(cu16(k) + b"".join(bytes(sigs[first + j]) for j in range(k)) + msgs[p])
+        sig0 = len(cu16(k))
+        msg0 = sig0 + 64 * k
+        kind = "valid"
+        if u[p] < malformed_frac:
+            kind = MALFORMED_KINDS[int(rng.integers(0, len(MALFORMED_KINDS)))]
+            if kind == "truncated":
+                tx = tx[:int(rng.integers(0, msg0 + 4))]
+            elif kind == "count_mismatch":
+                tx[msg0 + (1 if tx[msg0] & 0x80 else 0)] = (k % 4) + 1 if k < 4 else 1
+            elif kind == "zero_signatures":
+                tx = bytearray(b"\x00") + tx[sig0:]
+            elif kind == "few_keys":
+                h = msg0 + (1 if tx[msg0] & 0x80 else 0)
+                tx[h + 3] = k - 1            # fewer keys than signatures (count < 128)
+            elif kind == "bad_version":
+                if tx[msg0] & 0x80:
+                    tx[msg0] = 0x81
+                else:
+                    tx = tx[:msg0] + bytearray([0x82]) + tx[msg0:]
+            elif kind == "redundant_cu16":
+                tx = bytearray([k | 0x80, 0x00]) + tx[sig0:]
+            elif kind == "len_over_stride":
+                pass
+        elif u[p] < malformed_frac + corrupt_frac:
+            if rng.random() < 0.5:
+                kind = "corrupt_sig"
+                j = int(rng.integers(0, k))
+                bit = int(rng.integers(0, 512))
+                tx[sig0 + 64 * j + bit // 8] ^= 1 << (bit % 8)
+            else:
+                kind = "corrupt_msg"
+                bit = int(rng.integers(0, 8 * (len(tx) - msg0)))
+                tx[msg0 + bit // 8] ^= 1 << (bit % 8)
+        tx = bytes(tx[:stride])
+        data[p, :len(tx)] = np.frombuffer(tx, dtype=np.uint8)
+        plen[p] = len(tx) if kind != "len_over_stride" else stride + 1
+        kinds.append(kind)
+        first += k
+    return WirePackets(data, stride, plen, kinds)
