@@ -433,6 +433,87 @@ def bench_ragged_sigs(lib, torch):
             "results_identical_per_call_vs_batched": True, "valid_class_all_accepted": valid_ok}
 
 
+def bench_wire_packets(lib, torch, nthreads, n=16384, reps=5):
+    """Solana wire-format packets (16384 slots of 1280 bytes; legacy and
+    version-0 transactions with 1..4 signers; 5% corrupted, 3% malformed):
+    parse + verify on the device (gb300_packets.h) against the caller-side
+    flow the reference expects (parse on the host, then ed25519_verify_many
+    with 16 bytes of offsets per signature)."""
+    import workloads
+    from cuda_crypt import SigPackets
+    from oracle.oracle import get_oracle
+    t0 = time.perf_counter()
+    w = workloads.wire_packets(lib.create_keypairs, lib.sign_many, n=n, seed=17)
+    gen_s = time.perf_counter() - t0
+    stride = w.stride
+    # host path: gb300_ed25519_verify_packets (packets and lengths copied in, verdicts out)
+    lib.verify_packets(w.data, w.lens)
+    out, counts = lib.verify_packets(w.data, w.lens)
+    times = []
+    for _ in range(reps):
+        t = time.perf_counter()
+        lib.verify_packets(w.data, w.lens)
+        times.append(time.perf_counter() - t)
+    e2e_s = float(np.median(times))
+    nsig = int(counts.sum())
+    # device-resident: CUDA events on the launching stream, L2 flushed between launches
+    stream = torch.cuda.current_stream()
+    d = torch.from_numpy(w.data.ravel().copy()).cuda()
+    dl = torch.from_numpy(w.lens.astype(np.int32)).cuda()
+    ws = torch.empty(lib.packets_workspace_size(n, stride), dtype=torch.uint8, device="cuda")
+    dout = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
+    lib.verify_packets_device(d, stride, dl, ws, dout, None, stream.cuda_stream)
+    dev = []
+    for _ in range(reps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        lib.verify_packets_device(d, stride, dl, ws, dout, None, stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        dev.append(e0.elapsed_time(e1) * 1e-3)
+    dev_s = float(np.median(dev))
+    assert np.array_equal(dout.cpu().numpy(), out)
+    # the caller-side flow: host parse, then the per-signature offsets call
+    o = get_oracle()
+    t = time.perf_counter()
+    c2, ml, ko, so, mo = o.wire_offsets(w.data, stride, w.lens)
+    parse_s = time.perf_counter() - t
+    sp = SigPackets([w.data.ravel()], stride, ml, ko, so, mo)
+    lib.verify_many(sp)
+    vt = []
+    for _ in range(reps):
+        t = time.perf_counter()
+        per_sig = lib.verify_many(sp)
+        vt.append(time.perf_counter() - t)
+    offsets_e2e_s = float(np.median(vt))
+    pkt = np.repeat(np.arange(n), c2)
+    bad = np.zeros(n, dtype=np.int64)
+    np.add.at(bad, pkt, (per_sig == 0).astype(np.int64))
+    same = bool(np.array_equal(((c2 > 0) & (bad == 0)).astype(np.uint8), out) and np.array_equal(c2, counts))
+    # CPU baseline: the oracle parses and verifies the whole batch on all host cores
+    t = time.perf_counter()
+    cpu_out, _, _ = o.verify_wire_packets(w.data, stride, w.lens, nthreads)
+    cpu_s = time.perf_counter() - t
+    assert np.array_equal(cpu_out, out)
+    return {"metric": "wire packets verified/s", "unit": "packets/s",
+            "config": {"workload": f"{n} Solana wire-format packets in {stride}-byte slots (legacy and v0 messages, "
+                                   "1..4 signers; 5% corrupted, 3% malformed; seeded)",
+                       "packets": n, "signatures": nsig, "packet_bytes": n * stride, "generation_s": gen_s},
+            "value": n / dev_s, "device_s": dev_s, "signatures_per_s": nsig / dev_s,
+            "e2e": {"value": n / e2e_s, "unit": "packets/s", "s": e2e_s,
+                    "h2d_bytes_per_step": n * stride + 4 * n, "d2h_bytes_per_step": 5 * n,
+                    "path": "gb300_ed25519_verify_packets (host buffers)"},
+            "host_parse_then_verify_many": {"parse_s": parse_s, "verify_many_e2e_s": offsets_e2e_s,
+                                            "value": n / (parse_s + offsets_e2e_s), "unit": "packets/s",
+                                            "h2d_bytes_per_step": n * stride + 16 * nsig,
+                                            "parse": "oracle C parse on 1 host thread (the caller's work)"},
+            "results_identical_device_parse_vs_host_parse": same,
+            "cpu_baseline": {"value": n / cpu_s, "unit": "packets/s", "cores": nthreads, "kind": "port",
+                             "sample": f"the full batch ({nsig} signatures), CPU oracle parse + verify"}}
+
+
 def _pct(xs, q):
     return float(np.percentile(np.asarray(xs), q)) if len(xs) else None
 
@@ -747,6 +828,7 @@ def run_ours(args):
     if not args.skip_ragged:
         line["poh_ragged"] = bench_poh_ragged(lib, torch, steps=2)
         line["ragged_sigs"] = bench_ragged_sigs(lib, torch)
+        line["wire_packets"] = bench_wire_packets(lib, torch, nthreads)
     if not args.skip_serving:
         line["serving"] = bench_serving(lib)
     line["autotuner"] = lib.tuning()
