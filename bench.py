@@ -446,6 +446,9 @@ def bench_wire_packets(lib, torch, nthreads, n=16384, reps=5):
     w = workloads.wire_packets(lib.create_keypairs, lib.sign_many, n=n, seed=17)
     gen_s = time.perf_counter() - t0
     stride = w.stride
+    # packet memory page-locked with cuda_host_register, as the reference's
+    # callers do (verify.cu:349-355): both host paths copy it straight in
+    lib.host_register(w.data)
     # host path: gb300_ed25519_verify_packets (packets and lengths copied in, verdicts out)
     lib.verify_packets(w.data, w.lens)
     out, counts = lib.verify_packets(w.data, w.lens)
@@ -492,6 +495,7 @@ def bench_wire_packets(lib, torch, nthreads, n=16384, reps=5):
     bad = np.zeros(n, dtype=np.int64)
     np.add.at(bad, pkt, (per_sig == 0).astype(np.int64))
     same = bool(np.array_equal(((c2 > 0) & (bad == 0)).astype(np.uint8), out) and np.array_equal(c2, counts))
+    lib.host_unregister(w.data)
     # CPU baseline: the oracle parses and verifies the whole batch on all host cores
     t = time.perf_counter()
     cpu_out, _, _ = o.verify_wire_packets(w.data, stride, w.lens, nthreads)
@@ -504,7 +508,7 @@ def bench_wire_packets(lib, torch, nthreads, n=16384, reps=5):
             "value": n / dev_s, "device_s": dev_s, "signatures_per_s": nsig / dev_s,
             "e2e": {"value": n / e2e_s, "unit": "packets/s", "s": e2e_s,
                     "h2d_bytes_per_step": n * stride + 4 * n, "d2h_bytes_per_step": 5 * n,
-                    "path": "gb300_ed25519_verify_packets (host buffers)"},
+                    "path": "gb300_ed25519_verify_packets (host buffers, page-locked)"},
             "host_parse_then_verify_many": {"parse_s": parse_s, "verify_many_e2e_s": offsets_e2e_s,
                                             "value": n / (parse_s + offsets_e2e_s), "unit": "packets/s",
                                             "h2d_bytes_per_step": n * stride + 16 * nsig,
