@@ -433,6 +433,32 @@ def bench_ragged_sigs(lib, torch):
             "results_identical_per_call_vs_batched": True, "valid_class_all_accepted": valid_ok}
 
 
+def bench_poh_saturation(lib, torch, peaks, hashes=2000):
+    """PoH kernel throughput when the chain count fills every sub-partition
+    (the 4096-chain workload uses 256 of 608): entries = 608 warps x 32
+    lanes x 4, uniform counts, plain path.  Shows the kernel's ALU-pipe
+    fraction once parallelism is not the cap."""
+    sms = lib.tuning()["sms"]
+    n = 4 * sms * 32 * 4
+    stream = torch.cuda.current_stream()
+    d_h = torch.randint(0, 256, (n, 32), dtype=torch.uint8, device="cuda")
+    d_c = torch.full((n,), hashes, dtype=torch.int64, device="cuda")
+    lib.poh_verify_device(d_h, d_c, stream.cuda_stream)
+    ts = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        lib.poh_verify_device(d_h, d_c, stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1) * 1e-3)
+    t = float(np.median(ts))
+    rate = n * hashes / t
+    return {"entries": n, "num_hashes": hashes, "hashes_per_s": rate, "s": t,
+            "kernel": "poh_verify_kernel (one warp per 32 chains, 4 warps per sub-partition)",
+            "alu_ops_per_s": rate * POH_OPS_PER_HASH, "frac_of_lop3_peak": rate * POH_OPS_PER_HASH / peaks["lop3"]}
+
+
 def bench_wire_packets(lib, torch, nthreads, n=16384, reps=5):
     """Solana wire-format packets (16384 slots of 1280 bytes; legacy and
     version-0 transactions with 1..4 signers; 5% corrupted, 3% malformed):
@@ -775,6 +801,7 @@ def run_ours(args):
         "clocks": poh["clocks"],
         "int_peaks_tops": {k: v / 1e12 for k, v in peaks.items()},
     })
+    line["roofline"]["saturated_parallelism"] = bench_poh_saturation(lib, torch, peaks)
 
     # ---- Ed25519 verify: the 1024-packet config and a GPU-filling batch ----
     sp, corrupted = make_verify_data(lib, VERIFY_N, seed=1)
