@@ -27,6 +27,7 @@
 #include "ed25519.h"
 #include "poh_verify.h"
 #include "gb300_packets.h"
+#include "gb300_diag.h"
 #include "kernels.h"
 #include "tables.cuh"
 #include "host_buffers.h"
@@ -723,6 +724,20 @@ int gb300_ed25519_verify_device(const uint8_t* packets, uint64_t packets_len, co
     SigBatch b{packets, packets_len, message_lens, public_key_offsets, signature_offsets,
                message_start_offsets, num, out, T};
     return (int)launch_ed25519_verify(b, static_cast<cudaStream_t>(stream));
+}
+
+int gb300_ed25519_verify_device_form(const uint8_t* packets, uint64_t packets_len, const uint32_t* message_lens,
+                                     const uint32_t* public_key_offsets, const uint32_t* signature_offsets,
+                                     const uint32_t* message_start_offsets, uint32_t num, uint8_t* out, int form,
+                                     void* stream) {
+    if (num == 0) return 0;
+    if (form != kVerifySingle && form != kVerifyQuad) return (int)cudaErrorInvalidValue;
+    const CurveTables* T = tables_for_current_device();
+    if (!T) return (int)cudaErrorNoDevice;
+    if (reinterpret_cast<uintptr_t>(packets) & 3u) return (int)cudaErrorMisalignedAddress;
+    SigBatch b{packets, packets_len, message_lens, public_key_offsets, signature_offsets,
+               message_start_offsets, num, out, T};
+    return (int)launch_ed25519_verify_form(b, static_cast<cudaStream_t>(stream), form);
 }
 
 int gb300_ed25519_sign_device(const uint8_t* packets, uint64_t packets_len, const uint32_t* message_lens,

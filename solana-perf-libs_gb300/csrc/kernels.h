@@ -23,8 +23,11 @@ struct SigBatch {
 };
 
 // Ed25519 verify: out[i] = 1 if signature i is valid under the reference's
-// acceptance rules, else 0.
+// acceptance rules, else 0.  Forms: one thread per signature, or four lanes
+// per signature (lower latency on batches that do not fill the GPU).
+enum VerifyForm : int { kVerifySingle = 0, kVerifyQuad = 1 };
 cudaError_t launch_ed25519_verify(const SigBatch& b, cudaStream_t s);
+cudaError_t launch_ed25519_verify_form(const SigBatch& b, cudaStream_t s, int form);
 
 // Ed25519 sign: out[64*i ..] = R || S.  The 64-byte private key (clamped a,
 // then the nonce prefix) sits at signature_offsets[i].

@@ -37,6 +37,7 @@
 namespace {
 
 #include "ed25519_ops.cuh"
+#include "verify_quad.cuh"
 
 __global__ void __launch_bounds__(VERIFY_THREADS, VERIFY_MIN_BLOCKS) ed25519_verify_kernel(SigBatch a) {
     __shared__ uint32_t sVB[VB_WORDS * VB_ENTRIES];
@@ -45,6 +46,19 @@ __global__ void __launch_bounds__(VERIFY_THREADS, VERIFY_MIN_BLOCKS) ed25519_ver
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     a.out[i] = verify_one(a, sVB, i) ? 1 : 0;
+}
+
+// Four lanes per signature (verify_quad.cuh): signature t / 4 on lane t % 4.
+// A quad leaves the kernel together (blockDim is a multiple of 4).
+__global__ void __launch_bounds__(VERIFY_THREADS, VERIFY_MIN_BLOCKS) ed25519_verify_quad_kernel(SigBatch a) {
+    __shared__ uint32_t sVB[VB_WORDS * VB_ENTRIES];
+    for (int k = threadIdx.x; k < VB_WORDS * VB_ENTRIES; k += blockDim.x) sVB[k] = a.tables->vb[k];
+    __syncthreads();
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t i = t >> 2, q = t & 3u;
+    if (i >= a.n) return;
+    const bool ok = verify_quad(a, sVB, i, q);
+    if (q == 0) a.out[i] = ok ? 1 : 0;
 }
 
 // 0 = the encoding decodes and is not of order dividing 4.
@@ -61,11 +75,22 @@ __global__ void check_small_order_kernel(const uint8_t* pts, uint8_t* out, uint3
 
 }  // namespace
 
-cudaError_t launch_ed25519_verify(const SigBatch& b, cudaStream_t s) {
+cudaError_t launch_ed25519_verify_form(const SigBatch& b, cudaStream_t s, int form) {
     if (b.n == 0) return cudaSuccess;
-    uint32_t blocks = (b.n + VERIFY_THREADS - 1) / VERIFY_THREADS;
-    ed25519_verify_kernel<<<blocks, VERIFY_THREADS, 0, s>>>(b);
+    if (form == kVerifyQuad) {
+        const uint64_t threads = 4ull * b.n;
+        if (threads > 0xffffffffull) return cudaErrorInvalidValue;
+        const uint32_t blocks = (uint32_t)((threads + VERIFY_THREADS - 1) / VERIFY_THREADS);
+        ed25519_verify_quad_kernel<<<blocks, VERIFY_THREADS, 0, s>>>(b);
+    } else {
+        const uint32_t blocks = (b.n + VERIFY_THREADS - 1) / VERIFY_THREADS;
+        ed25519_verify_kernel<<<blocks, VERIFY_THREADS, 0, s>>>(b);
+    }
     return cudaGetLastError();
+}
+
+cudaError_t launch_ed25519_verify(const SigBatch& b, cudaStream_t s) {
+    return launch_ed25519_verify_form(b, s, kVerifySingle);
 }
 
 cudaError_t launch_check_small_order(const uint8_t* points, uint8_t* out, uint32_t n, const CurveTables* tables,

@@ -141,6 +141,9 @@ class CudaCrypt:
         L.gb300_ed25519_verify_packets.argtypes = [ctypes.POINTER(GpuElems), ctypes.c_uint32, ctypes.c_uint32,
                                                    _u32p, _u8p, _u32p]
         L.gb300_ed25519_verify_packets.restype = ctypes.c_int
+        L.gb300_ed25519_verify_device_form.argtypes = [ctypes.c_void_p, ctypes.c_uint64] + [ctypes.c_void_p] * 4 + \
+            [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.gb300_ed25519_verify_device_form.restype = ctypes.c_int
 
     # ---- reference entry points ------------------------------------------
     def init(self) -> bool:
@@ -347,6 +350,18 @@ class CudaCrypt:
             out.data_ptr(), stream)
         if rc != 0:
             raise RuntimeError(f"gb300_ed25519_verify_device: cudaError {rc}")
+
+    VERIFY_SINGLE, VERIFY_QUAD = 0, 1
+
+    def verify_device_form(self, packets, message_lens, public_key_offsets, signature_offsets,
+                           message_start_offsets, out, form, stream=0) -> None:
+        """verify_device with the kernel form forced (diagnostic)."""
+        rc = self.lib.gb300_ed25519_verify_device_form(
+            packets.data_ptr(), packets.numel(), message_lens.data_ptr(), public_key_offsets.data_ptr(),
+            signature_offsets.data_ptr(), message_start_offsets.data_ptr(), message_lens.numel(),
+            out.data_ptr(), form, stream)
+        if rc != 0:
+            raise RuntimeError(f"gb300_ed25519_verify_device_form: cudaError {rc}")
 
     def sign_device(self, packets, message_lens, public_key_offsets, private_key_offsets, message_start_offsets,
                     out, stream=0) -> None:

@@ -1,0 +1,132 @@
+"""The four-lanes-per-signature verify kernel (verify_quad.cuh) against the
+golden verdicts, the oracle and the one-thread kernel, with the cases that
+exercise its own final check (R decoded and compared projectively instead
+of encode + byte compare): R with its sign bit flipped, every non-canonical
+y >= p, undecodable R, R set to other valid points and to every small-order
+encoding, partial quads and warps."""
+import numpy as np
+import pytest
+
+import workloads
+from conftest import nthreads
+from test_gpu_verify import pack_items
+
+pytestmark = pytest.mark.gpu
+
+P = 2 ** 255 - 19
+
+
+def run_form(lib, sp, form):
+    torch = pytest.importorskip("torch")
+    d = torch.from_numpy(sp.concatenated().copy()).cuda()
+    arrs = [torch.from_numpy(np.asarray(a, dtype=np.int64).astype(np.int32)).cuda()
+            for a in (sp.message_lens, sp.public_key_offsets, sp.signature_offsets, sp.message_start_offsets)]
+    out = torch.full((sp.total_signatures,), 7, dtype=torch.uint8, device="cuda")
+    lib.verify_device_form(d, *arrs, out, form, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def both_forms(lib, oracle, sp):
+    exp = oracle.verify_packets(sp, nthreads())
+    single = run_form(lib, sp, lib.VERIFY_SINGLE)
+    quad = run_form(lib, sp, lib.VERIFY_QUAD)
+    assert np.array_equal(single, exp)
+    assert np.array_equal(quad, exp)
+    return exp
+
+
+def test_quad_golden(lib, golden_ed):
+    cases = golden_ed["verify"]
+    items = [(bytes.fromhex(c["sig"]), bytes.fromhex(c["msg"]), bytes.fromhex(c["pk"])) for c in cases]
+    sp = pack_items(items, gap_seed=5)
+    exp = np.array([c["valid"] for c in cases], dtype=np.uint8)
+    for form in (lib.VERIFY_SINGLE, lib.VERIFY_QUAD):
+        got = run_form(lib, sp, form)
+        bad = [cases[i]["kind"] for i in np.nonzero(got != exp)[0]]
+        assert not bad, (form, bad)
+
+
+def test_quad_uniform_and_ragged(lib, oracle):
+    sp, corrupted = workloads.verify_uniform(oracle.create_keypairs, oracle.sign_packets, n=1024, seed=51)
+    exp = both_forms(lib, oracle, sp)
+    assert np.array_equal(exp.astype(bool), ~corrupted)
+    rs = workloads.ragged_sigs(oracle.create_keypairs, oracle.sign_packets, n_batches=4, total_packet_cap=300,
+                               seed=52)
+    for sp in rs.verify:
+        both_forms(lib, oracle, sp)
+
+
+def _valid_items(oracle, n, seed, msg_len=None):
+    rng = np.random.default_rng(seed)
+    pk, sk = oracle.create_keypairs(rng.integers(0, 256, (n, 32), dtype=np.uint8))
+    items = []
+    for i in range(n):
+        m = int(rng.integers(0, 300)) if msg_len is None else msg_len
+        msg = bytes(rng.integers(0, 256, m, dtype=np.uint8).tolist())
+        items.append((oracle.sign(msg, bytes(pk[i]), bytes(sk[i])), msg, bytes(pk[i])))
+    return items, rng
+
+
+def test_quad_r_variants(lib, oracle):
+    items, rng = _valid_items(oracle, 64, 53)
+    so = workloads.small_order_encodings()
+    cases = list(items)
+    for sig, msg, pk in items:
+        s = bytearray(sig)
+        s[31] ^= 0x80                                     # R's sign bit
+        cases.append((bytes(s), msg, pk))
+        s = bytearray(sig)
+        s[:32] = rng.integers(0, 256, 32, dtype=np.uint8).tobytes()     # random R (mostly undecodable)
+        cases.append((bytes(s), msg, pk))
+        s = bytearray(sig)
+        s[:32] = items[int(rng.integers(0, len(items)))][2]             # another valid point
+        cases.append((bytes(s), msg, pk))
+    sig, msg, pk = items[0]
+    for k in range(19):                                   # y = p + k, both sign bits
+        for sign in (0, 1):
+            y = P + k
+            enc = bytearray(y.to_bytes(32, "little"))
+            enc[31] |= sign << 7
+            cases.append((bytes(enc) + sig[32:], msg, pk))
+    for enc in so:                                        # every small-order R and A
+        cases.append((enc + sig[32:], msg, pk))
+        cases.append((sig, msg, enc))
+    sp = pack_items(cases, gap_seed=6)
+    exp = both_forms(lib, oracle, sp)
+    assert exp[:64].all() and not exp[64:64 + 3 * 64].all()
+
+
+def test_quad_message_lengths_and_random(lib, oracle):
+    rng2 = np.random.default_rng(55)
+    seeds = rng2.integers(0, 256, (1, 32), dtype=np.uint8)
+    pkk, skk = oracle.create_keypairs(seeds)
+    cases = []
+    for m in range(0, 260):
+        msg = bytes(rng2.integers(0, 256, m, dtype=np.uint8).tolist())
+        sig = oracle.sign(msg, bytes(pkk[0]), bytes(skk[0]))
+        cases.append((sig, msg, bytes(pkk[0])))
+        bad = bytearray(sig)
+        bad[int(rng2.integers(0, 64))] ^= 1 << int(rng2.integers(0, 8))
+        cases.append((bytes(bad), msg, bytes(pkk[0])))
+    for i in range(600):
+        sig = bytearray(rng2.integers(0, 256, 64, dtype=np.uint8).tolist())
+        if i % 2:
+            sig[63] &= 0x0F
+        cases.append((bytes(sig), b"x" * (i % 50), rng2.integers(0, 256, 32, dtype=np.uint8).tobytes()))
+    both_forms(lib, oracle, pack_items(cases, gap_seed=7))
+
+
+@pytest.mark.parametrize("n", [1, 3, 7, 33, 257])
+def test_quad_partial_quads_and_warps(lib, oracle, n):
+    items, _ = _valid_items(oracle, n, 56 + n, msg_len=40)
+    exp = both_forms(lib, oracle, pack_items(items, gap_seed=8))
+    assert exp.all()
+
+
+def test_verify_form_rejects_bad_form(lib):
+    torch = pytest.importorskip("torch")
+    z = torch.zeros(4, dtype=torch.int32, device="cuda")
+    out = torch.zeros(4, dtype=torch.uint8, device="cuda")
+    with pytest.raises(RuntimeError):
+        lib.verify_device_form(torch.zeros(256, dtype=torch.uint8, device="cuda"), z, z, z, z, out, 2)
