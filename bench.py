@@ -941,6 +941,16 @@ def run_case(case: str):
         pk = dev(sp.concatenated())
         for _ in range(3):
             lib.verify_device(pk, *arrs, out, stream.cuda_stream)
+    elif case in ("verify-1024-single", "verify-1024-quad"):
+        sp, _ = make_verify_data(lib, 1024, seed=7)
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        arrs = [dev(a.astype(np.int32)) for a in
+                (sp.message_lens, sp.public_key_offsets, sp.signature_offsets, sp.message_start_offsets)]
+        out = torch.zeros(sp.total_signatures, dtype=torch.uint8, device="cuda")
+        pk = dev(sp.concatenated())
+        form = lib.VERIFY_QUAD if case.endswith("quad") else lib.VERIFY_SINGLE
+        for _ in range(3):
+            lib.verify_device_form(pk, *arrs, out, form, stream.cuda_stream)
     else:
         raise SystemExit(f"unknown case {case}")
     torch.cuda.synchronize()
