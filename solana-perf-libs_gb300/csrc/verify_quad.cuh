@@ -22,19 +22,38 @@
 //     test has already rejected).  This removes the final inversion.
 // SHA-512 and the decode chains run on all four lanes of a quad.  The
 // verdicts are those of verify_one for every input.
+//
+// Every lane of the warp reaches every shuffle: a rejected signature keeps
+// computing (on whatever values it has) and only its verdict is cleared, so
+// the shuffles name the whole warp.  A mask of the quad alone made each
+// shuffle a warp-synchronising branch, and lane-indexed operand choices are
+// bit masks, not conditionals, so that the four lanes never diverge around a
+// multiplication.
 #pragma once
 
-// lanes of this thread's quad
-__device__ __forceinline__ uint32_t quad_mask() { return 0xfu << (threadIdx.x & 28u); }
+constexpr uint32_t kQuadAll = 0xffffffffu;
+
+// per-lane selection masks: sel[k] = all ones on lane k of the quad
+struct QuadSel {
+    uint32_t m0, m1, m2, m3;
+};
+__device__ __forceinline__ QuadSel quad_sel(uint32_t q) {
+    QuadSel s;
+    s.m0 = 0u - (uint32_t)(q == 0);
+    s.m1 = 0u - (uint32_t)(q == 1);
+    s.m2 = 0u - (uint32_t)(q == 2);
+    s.m3 = 0u - (uint32_t)(q == 3);
+    return s;
+}
 
 __device__ __forceinline__ void quad_gather4(const fe& m, fe& o0, fe& o1, fe& o2, fe& o3, uint32_t mask) {
 #pragma unroll
     for (int w = 0; w < 8; w++) {
         const uint32_t v = m.v[w];
-        o0.v[w] = __shfl_sync(mask, v, 0, 4);
-        o1.v[w] = __shfl_sync(mask, v, 1, 4);
-        o2.v[w] = __shfl_sync(mask, v, 2, 4);
-        o3.v[w] = __shfl_sync(mask, v, 3, 4);
+        o0.v[w] = __shfl_sync(kQuadAll, v, 0, 4);
+        o1.v[w] = __shfl_sync(kQuadAll, v, 1, 4);
+        o2.v[w] = __shfl_sync(kQuadAll, v, 2, 4);
+        o3.v[w] = __shfl_sync(kQuadAll, v, 3, 4);
     }
 }
 
@@ -42,25 +61,27 @@ __device__ __forceinline__ void quad_gather3(const fe& m, fe& o0, fe& o1, fe& o2
 #pragma unroll
     for (int w = 0; w < 8; w++) {
         const uint32_t v = m.v[w];
-        o0.v[w] = __shfl_sync(mask, v, 0, 4);
-        o1.v[w] = __shfl_sync(mask, v, 1, 4);
-        o2.v[w] = __shfl_sync(mask, v, 2, 4);
+        o0.v[w] = __shfl_sync(kQuadAll, v, 0, 4);
+        o1.v[w] = __shfl_sync(kQuadAll, v, 1, 4);
+        o2.v[w] = __shfl_sync(kQuadAll, v, 2, 4);
     }
 }
 
 __device__ __forceinline__ void quad_from(fe& r, const fe& m, int src, uint32_t mask) {
 #pragma unroll
-    for (int w = 0; w < 8; w++) r.v[w] = __shfl_sync(mask, m.v[w], src, 4);
+    for (int w = 0; w < 8; w++) r.v[w] = __shfl_sync(kQuadAll, m.v[w], src, 4);
 }
 
-// r = (a0, a1, a2, a3)[q]
-__device__ __forceinline__ void fe_pick4(fe& r, const fe& a0, const fe& a1, const fe& a2, const fe& a3, uint32_t q) {
+// r = (a0, a1, a2, a3)[q], branch-free
+__device__ __forceinline__ void fe_pick4(fe& r, const fe& a0, const fe& a1, const fe& a2, const fe& a3,
+                                         const QuadSel& q) {
 #pragma unroll
-    for (int w = 0; w < 8; w++) r.v[w] = q == 0 ? a0.v[w] : q == 1 ? a1.v[w] : q == 2 ? a2.v[w] : a3.v[w];
+    for (int w = 0; w < 8; w++)
+        r.v[w] = (a0.v[w] & q.m0) | (a1.v[w] & q.m1) | (a2.v[w] & q.m2) | (a3.v[w] & q.m3);
 }
 
 // Doubling, first stage (four squarings), all lanes get (E, F, G, H).
-__device__ __forceinline__ void qdbl(ge_done& r, const fe& X, const fe& Y, const fe& Z, uint32_t q, uint32_t mask) {
+__device__ __forceinline__ void qdbl(ge_done& r, const fe& X, const fe& Y, const fe& Z, const QuadSel& q, uint32_t mask) {
     fe s, op, m, a, b, c, ss;
     fe_add(s, X, Y);
     fe_pick4(op, X, Y, Z, s, q);
@@ -74,7 +95,7 @@ __device__ __forceinline__ void qdbl(ge_done& r, const fe& X, const fe& Y, const
 }
 
 // Second stage: X = EF, Y = GH, Z = FG (and T = EH).
-__device__ __forceinline__ void qto_p3(ge_p3& R, const ge_done& c, uint32_t q, uint32_t mask) {
+__device__ __forceinline__ void qto_p3(ge_p3& R, const ge_done& c, const QuadSel& q, uint32_t mask) {
     fe o1, o2, m;
     fe_pick4(o1, c.E, c.G, c.F, c.E, q);
     fe_pick4(o2, c.F, c.H, c.G, c.H, q);
@@ -82,7 +103,7 @@ __device__ __forceinline__ void qto_p3(ge_p3& R, const ge_done& c, uint32_t q, u
     quad_gather4(m, R.X, R.Y, R.Z, R.T, mask);
 }
 
-__device__ __forceinline__ void qto_p2(fe& X, fe& Y, fe& Z, const ge_done& c, uint32_t q, uint32_t mask) {
+__device__ __forceinline__ void qto_p2(fe& X, fe& Y, fe& Z, const ge_done& c, const QuadSel& q, uint32_t mask) {
     fe o1, o2, m;
     fe_pick4(o1, c.E, c.G, c.F, c.E, q);
     fe_pick4(o2, c.F, c.H, c.G, c.H, q);
@@ -106,7 +127,7 @@ __device__ __forceinline__ void qadd_finish(ge_done& r, const fe& m, bool neg, u
 // lane 0 (Y-X, Y+X), lane 1 (Y+X, Y-X), lane 2 (2dT, 2dT), lane 3 (2Z, 2Z);
 // the operand is c1 when subtracting, c0 when adding.
 __device__ __forceinline__ void qadd_cached(ge_done& r, const ge_p3& p, const fe& c0, const fe& c1, bool neg,
-                                            uint32_t q, uint32_t mask) {
+                                            const QuadSel& q, uint32_t mask) {
     fe ypx, ymx, o1, o2, m;
     fe_add(ypx, p.Y, p.X);
     fe_sub(ymx, p.Y, p.X);
@@ -120,23 +141,27 @@ __device__ __forceinline__ void qadd_cached(ge_done& r, const ge_p3& p, const fe
 // (y+x when subtracting), lane 1 y+x (y-x), lane 2 2dxy, lane 3 multiplies
 // Z by 2 (the affine addend has Z = 1).
 __device__ __forceinline__ void qadd_niels(ge_done& r, const ge_p3& p, const uint32_t* sVB, int e, bool neg,
-                                           uint32_t q, uint32_t mask) {
+                                           const QuadSel& q, uint32_t lane_q, uint32_t mask) {
     fe ypx, ymx, o1, o2, m;
     fe_add(ypx, p.Y, p.X);
     fe_sub(ymx, p.Y, p.X);
     fe_pick4(o1, ymx, ypx, p.T, p.Z, q);
-    const int comp = q == 0 ? (neg ? 0 : 1) : q == 1 ? (neg ? 1 : 0) : 2;   // 0 y+x, 1 y-x, 2 2dxy
+    // component read: lane 0 y-x (y+x when subtracting), lane 1 the other,
+    // lanes 2-3 2dxy (lane 3's operand is replaced by 2 below)
+    const uint32_t flip = (uint32_t)neg ^ (lane_q & 1u);
+    const int comp = lane_q >= 2 ? 2 : (int)(flip ^ 1u);          // 0 y+x, 1 y-x, 2 2dxy
+    const uint32_t two0 = 2u & q.m3;
 #pragma unroll
     for (int w = 0; w < 8; w++) {
         const uint32_t v = sVB[(comp * 8 + w) * VB_ENTRIES + e];
-        o2.v[w] = q == 3 ? (w == 0 ? 2u : 0u) : v;
+        o2.v[w] = (v & ~q.m3) | (w == 0 ? two0 : 0u);
     }
     fe_mul(m, o1, o2);
     qadd_finish(r, m, neg, mask);
 }
 
 // This lane's two components of the cached form of P.
-__device__ __forceinline__ void qcached_comps(fe& c0, fe& c1, const ge_p3& P, const fe& d2, uint32_t q) {
+__device__ __forceinline__ void qcached_comps(fe& c0, fe& c1, const ge_p3& P, const fe& d2, const QuadSel& q) {
     fe ypx, ymx, z2, t2d;
     fe_add(ypx, P.Y, P.X);
     fe_sub(ymx, P.Y, P.X);
@@ -154,15 +179,17 @@ __device__ __forceinline__ bool enc_y_canonical(const uint32_t w[8]) {
 }
 
 // Verdict of signature i, computed by the quad (every lane returns it).
-// All lanes of a quad take the same branches outside ge_decode, so the quad
-// reaches every shuffle together.
-__device__ bool verify_quad(const SigBatch& a, const uint32_t* sVB, uint32_t i, uint32_t q) {
-    const uint32_t mask = quad_mask();
-    const uint64_t so = a.signature_offsets[i];
-    const uint64_t po = a.public_key_offsets[i];
-    const uint64_t mo = a.message_start_offsets[i];
-    const uint32_t m = a.message_lens[i];
-    if (so + 64 > a.packets_len || po + 32 > a.packets_len || mo + m > a.packets_len) return false;
+// No lane leaves early: a rejected signature runs to the end with its
+// verdict already cleared, so every lane of the warp meets every shuffle.
+__device__ bool verify_quad(const SigBatch& a, const uint32_t* sVB, uint32_t i, uint32_t lane_q) {
+    const QuadSel q = quad_sel(lane_q);
+    const uint32_t mask = kQuadAll;
+    uint64_t so = a.signature_offsets[i];
+    uint64_t po = a.public_key_offsets[i];
+    uint64_t mo = a.message_start_offsets[i];
+    uint32_t m = a.message_lens[i];
+    bool ok = !(so + 64 > a.packets_len || po + 32 > a.packets_len || mo + m > a.packets_len);
+    if (!ok) so = po = mo = m = 0;                          // read nothing out of range
 
     uint32_t sig[16], pk[8];
 #pragma unroll
@@ -170,9 +197,9 @@ __device__ bool verify_quad(const SigBatch& a, const uint32_t* sVB, uint32_t i, 
 #pragma unroll
     for (int k = 0; k < 8; k++) pk[k] = ld_u32_any(a.packets, po + 4 * k, a.packets_len);
 
-    if (sig[15] & 0xf0000000u) return false;               // S >= 2^252
-    if (enc_is_order4(sig) || enc_is_order4(pk)) return false;
-    if (!enc_y_canonical(sig)) return false;                // R's y >= p: no canonical encoding equals it
+    ok = ok && !(sig[15] & 0xf0000000u);                    // S >= 2^252
+    ok = ok && !enc_is_order4(sig) && !enc_is_order4(pk);
+    ok = ok && enc_y_canonical(sig);                        // R's y >= p: no canonical encoding equals it
 
     // h = SHA-512(R || A || M) mod L
     uint64_t pre[8];
@@ -188,12 +215,13 @@ __device__ bool verify_quad(const SigBatch& a, const uint32_t* sVB, uint32_t i, 
     // lanes 0-1 decode A, lanes 2-3 decode R
     const CurveConsts& K = a.tables->K;
     uint32_t enc[8];
+    const uint32_t take_pk = 0u - (uint32_t)(lane_q < 2);
 #pragma unroll
-    for (int k = 0; k < 8; k++) enc[k] = q < 2 ? pk[k] : sig[k];
+    for (int k = 0; k < 8; k++) enc[k] = (pk[k] & take_pk) | (sig[k] & ~take_pk);
     fe dx, dy;
     const uint32_t dok = ge_decode(dx, dy, enc, K) ? 1u : 0u;
-    const uint32_t okA = __shfl_sync(mask, dok, 0, 4), okR = __shfl_sync(mask, dok, 2, 4);
-    if (!okA || !okR) return false;
+    const uint32_t okA = __shfl_sync(kQuadAll, dok, 0, 4), okR = __shfl_sync(kQuadAll, dok, 2, 4);
+    ok = ok && okA && okR;
     fe ax, ay, rx, ry;
     quad_from(ax, dx, 0, mask);
     quad_from(ay, dy, 0, mask);
@@ -285,7 +313,7 @@ __device__ bool verify_quad(const SigBatch& a, const uint32_t* sVB, uint32_t i, 
             int bn = (k < 31) ? (int)((scar >> (k + 1)) & 1u) : 0;
             int db = byte + bc - 256 * bn;
             int ub = min(db < 0 ? -db : db, VB_ENTRIES - 1);
-            qadd_niels(t, R, sVB, ub, db < 0, q, mask);
+            qadd_niels(t, R, sVB, ub, db < 0, q, lane_q, mask);
         }
         qto_p2(R.X, R.Y, R.Z, t, q, mask);
     }
@@ -296,5 +324,5 @@ __device__ bool verify_quad(const SigBatch& a, const uint32_t* sVB, uint32_t i, 
     fe_mul(prod, o1, R.Z);
     quad_from(xz, prod, 0, mask);
     quad_from(yz, prod, 1, mask);
-    return fe_equal(R.X, xz) && fe_equal(R.Y, yz);
+    return ok && fe_equal(R.X, xz) && fe_equal(R.Y, yz);
 }
