@@ -72,6 +72,12 @@ __device__ __forceinline__ void quad_from(fe& r, const fe& m, int src, uint32_t 
     for (int w = 0; w < 8; w++) r.v[w] = __shfl_sync(kQuadAll, m.v[w], src, 4);
 }
 
+// r = msk ? b : a, branch-free (msk all ones or zero)
+__device__ __forceinline__ void fe_select_m(fe& r, const fe& a, const fe& b, uint32_t msk) {
+#pragma unroll
+    for (int w = 0; w < 8; w++) r.v[w] = (b.v[w] & msk) | (a.v[w] & ~msk);
+}
+
 // r = (a0, a1, a2, a3)[q], branch-free
 __device__ __forceinline__ void fe_pick4(fe& r, const fe& a0, const fe& a1, const fe& a2, const fe& a3,
                                          const QuadSel& q) {
@@ -119,8 +125,9 @@ __device__ __forceinline__ void qadd_finish(ge_done& r, const fe& m, bool neg, u
     fe_add(r.H, b, a);
     fe_sub(f, d, c);
     fe_add(g, d, c);
-    fe_select(r.F, f, g, neg);
-    fe_select(r.G, g, f, neg);
+    const uint32_t nm = 0u - (uint32_t)neg;
+    fe_select_m(r.F, f, g, nm);
+    fe_select_m(r.G, g, f, nm);
 }
 
 // p +- k(-A): the lane's own components of the cached entry, (c0, c1) =
@@ -132,7 +139,7 @@ __device__ __forceinline__ void qadd_cached(ge_done& r, const ge_p3& p, const fe
     fe_add(ypx, p.Y, p.X);
     fe_sub(ymx, p.Y, p.X);
     fe_pick4(o1, ymx, ypx, p.T, p.Z, q);
-    fe_select(o2, c0, c1, neg);
+    fe_select_m(o2, c0, c1, 0u - (uint32_t)neg);
     fe_mul(m, o1, o2);
     qadd_finish(r, m, neg, mask);
 }
