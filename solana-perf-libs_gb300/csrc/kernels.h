@@ -74,6 +74,9 @@ struct SigWork {
     // kernel verifies *count_dev items (v.n and total_chunks are then the
     // capacity, used only to size the grid).
     const uint32_t* count_dev = nullptr;
+    // Set by launch_sig_batch: verify chunks of 8 signatures, four lanes each
+    // (small batches); otherwise chunks of 32, one lane each.
+    bool v_quad = false;
 };
 cudaError_t launch_sig_batch(const SigWork& w, int threads, int blocks_per_sm, int sms, cudaStream_t s);
 

@@ -13,6 +13,7 @@
 //     chunks (early rejections, short messages) simply takes more;
 //   * each block stages the verify basepoint table into shared memory once.
 #include <cuda_runtime.h>
+#include <cstdlib>
 #include "kernels.h"
 #include "tables.cuh"
 #include "sha512.cuh"
@@ -21,6 +22,16 @@
 namespace {
 
 #include "ed25519_ops.cuh"
+#include "verify_quad.cuh"
+
+// Chunk counts of a launch: verify chunks (32 signatures, or 8 in quad
+// mode), then sign chunks of 32.
+__host__ __device__ __forceinline__ uint32_t verify_chunks(const SigWork& w, uint32_t vn) {
+    return w.count_dev ? (vn + 31u) / 32u : w.v_quad ? (vn + 7u) / 8u : w.sign_base / 32u;
+}
+__host__ __device__ __forceinline__ uint32_t sign_chunks(const SigWork& w) {
+    return w.count_dev ? 0u : w.total_chunks - w.sign_base / 32u;
+}
 
 template <int T>
 __global__ void __launch_bounds__(T) sig_persistent_kernel(SigWork w) {
@@ -29,18 +40,26 @@ __global__ void __launch_bounds__(T) sig_persistent_kernel(SigWork w) {
     __syncthreads();
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t vn = w.count_dev ? *w.count_dev : w.v.n;
-    const uint32_t chunks = w.count_dev ? (vn + 31u) / 32u : w.total_chunks;
+    const uint32_t vchunks = verify_chunks(w, vn);
+    const uint32_t chunks = vchunks + sign_chunks(w);
     for (;;) {
         uint32_t c = 0;
         if (lane == 0) c = atomicAdd(w.next, 1u);
         c = __shfl_sync(0xffffffffu, c, 0);
         if (c >= chunks) break;
-        const uint32_t start = c * 32u;
-        if (start < w.sign_base) {
-            const uint32_t i = start + lane;
-            if (i < vn) w.v.out[i] = verify_one(w.v, sVB, i) ? 1 : 0;
+        if (c < vchunks) {
+            if (w.v_quad) {
+                // every lane runs an item (past the end: the last one again,
+                // result dropped) so the whole warp meets every shuffle
+                const uint32_t i = c * 8u + (lane >> 2);
+                const bool ok = verify_quad(w.v, sVB, i < vn ? i : vn - 1u, lane & 3u);
+                if (i < vn && (lane & 3u) == 0) w.v.out[i] = ok ? 1 : 0;
+            } else {
+                const uint32_t i = c * 32u + lane;
+                if (i < vn) w.v.out[i] = verify_one(w.v, sVB, i) ? 1 : 0;
+            }
         } else {
-            const uint32_t i = start - w.sign_base + lane;
+            const uint32_t i = (c - vchunks) * 32u + lane;
             if (i < w.s.n) sign_one(w.s, i);
         }
     }
@@ -53,7 +72,7 @@ cudaError_t launch_t(const SigWork& w, int blocks_per_sm, int sms, cudaStream_t 
     if (e != cudaSuccess) return e;
     if (maxb < 1) maxb = 1;
     int b = blocks_per_sm < 1 ? maxb : (blocks_per_sm < maxb ? blocks_per_sm : maxb);
-    uint32_t warps_needed = w.total_chunks;
+    uint32_t warps_needed = verify_chunks(w, w.v.n) + sign_chunks(w);
     uint32_t grid = (uint32_t)(b * sms);
     uint32_t per_block = T / 32;
     if (grid * per_block > warps_needed) grid = (warps_needed + per_block - 1) / per_block;
@@ -64,8 +83,14 @@ cudaError_t launch_t(const SigWork& w, int blocks_per_sm, int sms, cudaStream_t 
 
 }  // namespace
 
-cudaError_t launch_sig_batch(const SigWork& w, int threads, int blocks_per_sm, int sms, cudaStream_t s) {
-    if (w.total_chunks == 0) return cudaSuccess;
+// Verify signatures four lanes each while the batch leaves the GPU idle
+// (the same size rule as launch_ed25519_verify: up to 64 per SM).
+cudaError_t launch_sig_batch(const SigWork& w_in, int threads, int blocks_per_sm, int sms, cudaStream_t s) {
+    if (w_in.total_chunks == 0) return cudaSuccess;
+    SigWork w = w_in;
+    static const int forced = getenv("GB300_CRYPT_VERIFY_FORM") ? atoi(getenv("GB300_CRYPT_VERIFY_FORM")) : -1;
+    w.v_quad = !w.count_dev && w.v.n > 0 &&
+               (forced == kVerifyQuad || (forced != kVerifySingle && (uint64_t)w.v.n <= 64ull * (uint64_t)sms));
     cudaError_t e = cudaMemsetAsync(w.next, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     switch (threads) {

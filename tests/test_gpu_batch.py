@@ -168,3 +168,17 @@ def test_poh_batch_shape_rejects_bad_shapes(lib):
     for warps, form in ((0, 0), (64, 5), (64, -1), (10 ** 6, 0)):
         with pytest.raises(RuntimeError):
             lib.poh_verify_batch_shape(dh, dc, ws, warps, form)
+
+
+def test_sig_batch_both_verify_modes(lib, oracle):
+    """The persistent launch verifies four lanes per signature up to 64 per
+    SM and one lane per signature above: a batch on each side of the rule,
+    against the oracle."""
+    sms = lib.tuning()["sms"]
+    for n in (8 * sms, 64 * sms + 100):
+        sp, corrupted = workloads.verify_uniform(lib.create_keypairs, lib.sign_many, n=n, seed=70 + n % 7)
+        exp = oracle.verify_packets(sp, nthreads())
+        got = lib.ed25519_batch([(sp, JOB_VERIFY)])[0]
+        assert np.array_equal(got, exp), n
+        assert np.array_equal(lib.verify_many(sp), exp), n
+        assert np.array_equal(got.astype(bool), ~corrupted)
