@@ -77,6 +77,8 @@ struct SigWork {
     // Set by launch_sig_batch: verify chunks of 8 signatures, four lanes each
     // (small batches); otherwise chunks of 32, one lane each.
     bool v_quad = false;
+    // Caller's choice: -1 by batch size, kVerifySingle / kVerifyQuad to force.
+    int v_form_hint = -1;
 };
 cudaError_t launch_sig_batch(const SigWork& w, int threads, int blocks_per_sm, int sms, cudaStream_t s);
 

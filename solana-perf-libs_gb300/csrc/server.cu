@@ -116,7 +116,10 @@ uint64_t sig_bytes(const gb300_sig_job& j) {
 }
 
 // Stage and launch the requests in S.reqs (signature jobs) on S.stream.
-cudaError_t launch_sigs(gb300_server* sv, Slot& S) {
+// alone: no other signature launch in flight.  Four lanes per signature
+// lower a small launch's latency but halve its throughput, so they are used
+// only when the launch has the GPU's signature capacity to itself.
+cudaError_t launch_sigs(gb300_server* sv, Slot& S, bool alone) {
     uint64_t nv = 0, ns = 0, total = 0;
     bool locked = true;
     for (auto& r : S.reqs) {
@@ -180,6 +183,7 @@ cudaError_t launch_sigs(gb300_server* sv, Slot& S) {
     w.sign_base = (uint32_t)((nv + 31) / 32 * 32);
     w.total_chunks = (uint32_t)((w.sign_base + ns + 31) / 32);
     w.next = static_cast<uint32_t*>(S.d_scratch.p);
+    w.v_form_hint = alone ? -1 : kVerifySingle;
     if ((e = launch_sig_batch(w, sv->info.sig_threads, sv->info.sig_blocks_per_sm, sv->info.sms, S.stream)) !=
         cudaSuccess)
         return e;
@@ -308,8 +312,10 @@ void dispatcher(gb300_server* sv) {
             sv->launches_sig++;
             if (S.reqs.size() > sv->merged_max) sv->merged_max = S.reqs.size();
             S.t_admit = now_ns();
+            bool alone = true;
+            for (auto& O : sv->sig_slots) alone = alone && (&O == &S || !O.busy);
             lk.unlock();
-            S.err = launch_sigs(sv, S);
+            S.err = launch_sigs(sv, S, alone);
             S.t_enqueued = now_ns();
             lk.lock();
             launched = true;

@@ -89,8 +89,9 @@ cudaError_t launch_sig_batch(const SigWork& w_in, int threads, int blocks_per_sm
     if (w_in.total_chunks == 0) return cudaSuccess;
     SigWork w = w_in;
     static const int forced = getenv("GB300_CRYPT_VERIFY_FORM") ? atoi(getenv("GB300_CRYPT_VERIFY_FORM")) : -1;
+    const int form = (forced == kVerifySingle || forced == kVerifyQuad) ? forced : w.v_form_hint;
     w.v_quad = !w.count_dev && w.v.n > 0 &&
-               (forced == kVerifyQuad || (forced != kVerifySingle && (uint64_t)w.v.n <= 64ull * (uint64_t)sms));
+               (form == kVerifyQuad || (form != kVerifySingle && (uint64_t)w.v.n <= 64ull * (uint64_t)sms));
     cudaError_t e = cudaMemsetAsync(w.next, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     switch (threads) {
