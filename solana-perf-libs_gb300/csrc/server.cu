@@ -116,10 +116,7 @@ uint64_t sig_bytes(const gb300_sig_job& j) {
 }
 
 // Stage and launch the requests in S.reqs (signature jobs) on S.stream.
-// alone: no other signature launch in flight.  Four lanes per signature
-// lower a small launch's latency but halve its throughput, so they are used
-// only when the launch has the GPU's signature capacity to itself.
-cudaError_t launch_sigs(gb300_server* sv, Slot& S, bool alone) {
+cudaError_t launch_sigs(gb300_server* sv, Slot& S) {
     uint64_t nv = 0, ns = 0, total = 0;
     bool locked = true;
     for (auto& r : S.reqs) {
@@ -183,7 +180,6 @@ cudaError_t launch_sigs(gb300_server* sv, Slot& S, bool alone) {
     w.sign_base = (uint32_t)((nv + 31) / 32 * 32);
     w.total_chunks = (uint32_t)((w.sign_base + ns + 31) / 32);
     w.next = static_cast<uint32_t*>(S.d_scratch.p);
-    w.v_form_hint = alone ? -1 : kVerifySingle;
     if ((e = launch_sig_batch(w, sv->info.sig_threads, sv->info.sig_blocks_per_sm, sv->info.sms, S.stream)) !=
         cudaSuccess)
         return e;
@@ -312,10 +308,8 @@ void dispatcher(gb300_server* sv) {
             sv->launches_sig++;
             if (S.reqs.size() > sv->merged_max) sv->merged_max = S.reqs.size();
             S.t_admit = now_ns();
-            bool alone = true;
-            for (auto& O : sv->sig_slots) alone = alone && (&O == &S || !O.busy);
             lk.unlock();
-            S.err = launch_sigs(sv, S, alone);
+            S.err = launch_sigs(sv, S);
             S.t_enqueued = now_ns();
             lk.lock();
             launched = true;
