@@ -35,9 +35,10 @@ int gb300_poh_verify_batch_shape(uint8_t* hashes, const uint64_t* num_hashes, ui
                                  size_t workspace_bytes, int warps, int form, void* stream);
 
 /* gb300_ed25519_verify_device with the kernel form forced instead of picked
- * by batch size: form 0 one thread per signature, 1 four lanes per signature.
- * Same verdicts either way; used to test and time each form.  Returns a
- * cudaError_t. */
+ * by batch size: form 0 one thread per signature (the tuned window width of
+ * h), 1 four lanes per signature, 2 one thread per signature with a 4-bit
+ * window, 3 the same with a 5-bit window.  Same verdicts in every form; used
+ * to test and time each.  Returns a cudaError_t. */
 int gb300_ed25519_verify_device_form(const uint8_t* packets, uint64_t packets_len, const uint32_t* message_lens,
                                      const uint32_t* public_key_offsets, const uint32_t* signature_offsets,
                                      const uint32_t* message_start_offsets, uint32_t num, uint8_t* out, int form,

@@ -89,9 +89,10 @@ struct Queue {
 struct Tuning {
     int sig_threads = 128;        // threads per block of the persistent sign/verify kernel
     int sig_blocks_per_sm = 0;    // 0 = as many as fit
+    int verify_window = 4;        // signed window width of h in the one-lane verify (4 or 5)
     int poh_warps_per_smsp = 1;   // resident warps of the persistent PoH kernel per SM sub-partition
     int poh_form = kPohSingle;    // PohBatchForm of ragged PoH batches
-    double sig_ms[3] = {0, 0, 0}; // calibration times for 64 / 128 / 256 threads
+    double sig_ms[2][3] = {{0, 0, 0}, {0, 0, 0}};  // calibration: window 4 / 5 x 64 / 128 / 256 threads
     double poh_ms[4] = {0, 0, 0, 0};  // calibration: single and paired forms, 1 and 2 warps per sub-partition
     int calib_sigs = 0, calib_chains = 0;
 };
@@ -103,6 +104,7 @@ struct Device {
     Queue q[kQueues];
     uint32_t next_queue = 0;
     std::once_flag tuned;
+    std::atomic<bool> tuned_done{false};
     Tuning tune;
 };
 
@@ -324,19 +326,23 @@ void tune_device(Device& D) {
         w.next = dq;
         const int cand[3] = {64, 128, 256};
         double best = 1e30;
-        for (int c = 0; c < 3; c++) {
-            cudaError_t err = cudaSuccess;
-            launch_sig_batch(w, cand[c], 0, sms, s);   // warm
-            cudaStreamSynchronize(s);
-            float ms = 1e30f;
-            for (int r = 0; r < 2; r++) {
-                float t = time_ms(s, [&]() { return launch_sig_batch(w, cand[c], 0, sms, s); }, err);
-                if (err == cudaSuccess && t < ms) ms = t;
-            }
-            T.sig_ms[c] = ms;
-            if (ms < best) {
-                best = ms;
-                T.sig_threads = cand[c];
+        for (int wi = 0; wi < 2; wi++) {
+            w.v.window = 4 + wi;
+            for (int c = 0; c < 3; c++) {
+                cudaError_t err = cudaSuccess;
+                launch_sig_batch(w, cand[c], 0, sms, s);   // warm
+                cudaStreamSynchronize(s);
+                float ms = 1e30f;
+                for (int r = 0; r < 2; r++) {
+                    float t = time_ms(s, [&]() { return launch_sig_batch(w, cand[c], 0, sms, s); }, err);
+                    if (err == cudaSuccess && t < ms) ms = t;
+                }
+                T.sig_ms[wi][c] = ms;
+                if (ms < best) {
+                    best = ms;
+                    T.sig_threads = cand[c];
+                    T.verify_window = 4 + wi;
+                }
             }
         }
         T.calib_sigs = (int)(nv + ns);
@@ -383,10 +389,12 @@ void tune_device(Device& D) {
     cudaStreamDestroy(s);
     T.sig_threads = env_int("GB300_CRYPT_SIG_THREADS", T.sig_threads);
     T.sig_blocks_per_sm = env_int("GB300_CRYPT_SIG_BLOCKS", T.sig_blocks_per_sm);
+    T.verify_window = env_int("GB300_CRYPT_VERIFY_WINDOW", T.verify_window) == 5 ? 5 : 4;
     T.poh_warps_per_smsp = env_int("GB300_CRYPT_POH_WARPS_PER_SMSP", T.poh_warps_per_smsp);
     T.poh_form = env_int("GB300_CRYPT_POH_PAIRED", T.poh_form == kPohPair) ? kPohPair : kPohSingle;
-    LOG("tuned gpu %d: sig threads %d (ms %.3f %.3f %.3f), poh warps/smsp %d %s (ms %.3f %.3f %.3f %.3f)\n", D.id,
-        T.sig_threads, T.sig_ms[0], T.sig_ms[1], T.sig_ms[2], T.poh_warps_per_smsp,
+    LOG("tuned gpu %d: sig threads %d window %d (ms %.3f %.3f %.3f / %.3f %.3f %.3f), poh warps/smsp %d %s "
+        "(ms %.3f %.3f %.3f %.3f)\n", D.id, T.sig_threads, T.verify_window, T.sig_ms[0][0], T.sig_ms[0][1],
+        T.sig_ms[0][2], T.sig_ms[1][0], T.sig_ms[1][1], T.sig_ms[1][2], T.poh_warps_per_smsp,
         T.poh_form == kPohPair ? "paired" : "single", T.poh_ms[0], T.poh_ms[1], T.poh_ms[2], T.poh_ms[3]);
 }
 
@@ -405,9 +413,15 @@ const Tuning& tuning_for(Device& D) {
         cudaSetDevice(D.id);
         tune_device(D);
         if (prev >= 0) cudaSetDevice(prev);
+        D.tuned_done.store(true);
     });
     return D.tune;
 }
+
+// The tuned verify window when the device has been tuned, else 4: the
+// one-call device entry points do not start the tuner (it allocates and
+// synchronises, which a caller capturing a graph cannot allow).
+int verify_window_if_tuned(Device& D) { return D.tuned_done.load() ? D.tune.verify_window : 4; }
 
 // Stages one signature batch, runs verify or sign on it and copies the
 // results into `out` (n bytes, or 64n bytes for signing).
@@ -467,6 +481,7 @@ cudaError_t run_sig_batch(Lease& L, cudaStream_t s, bool sign, const gpu_Elems* 
     b.n = n;
     b.out = static_cast<uint8_t*>(Q.d_out.p);
     b.tables = L.dev->tables;
+    b.window = tuning_for(*L.dev).verify_window;
     TRY(sign ? launch_ed25519_sign(b, s) : launch_ed25519_verify(b, s));
     TRY(cudaMemcpyAsync(Q.h_out.p, Q.d_out.p, out_bytes, cudaMemcpyDeviceToHost, s));
     TRY(cudaStreamSynchronize(s));
@@ -520,6 +535,7 @@ bool crypt_device_info(int dev, CryptDeviceInfo* out) {
     out->sms = D->sms;
     out->sig_threads = T.sig_threads;
     out->sig_blocks_per_sm = T.sig_blocks_per_sm;
+    out->verify_window = T.verify_window;
     out->poh_warps = 4 * D->sms * T.poh_warps_per_smsp;
     return true;
 }
@@ -718,11 +734,12 @@ int gb300_ed25519_verify_device(const uint8_t* packets, uint64_t packets_len, co
                                 const uint32_t* message_start_offsets, uint32_t num, uint8_t* out,
                                 void* stream) {
     if (num == 0) return 0;
-    const CurveTables* T = tables_for_current_device();
-    if (!T) return (int)cudaErrorNoDevice;
+    Device* D = current_device();
+    if (!D) return (int)cudaErrorNoDevice;
     if (reinterpret_cast<uintptr_t>(packets) & 3u) return (int)cudaErrorMisalignedAddress;
     SigBatch b{packets, packets_len, message_lens, public_key_offsets, signature_offsets,
-               message_start_offsets, num, out, T};
+               message_start_offsets, num, out, D->tables};
+    b.window = verify_window_if_tuned(*D);
     return (int)launch_ed25519_verify(b, static_cast<cudaStream_t>(stream));
 }
 
@@ -731,13 +748,15 @@ int gb300_ed25519_verify_device_form(const uint8_t* packets, uint64_t packets_le
                                      const uint32_t* message_start_offsets, uint32_t num, uint8_t* out, int form,
                                      void* stream) {
     if (num == 0) return 0;
-    if (form != kVerifySingle && form != kVerifyQuad) return (int)cudaErrorInvalidValue;
-    const CurveTables* T = tables_for_current_device();
-    if (!T) return (int)cudaErrorNoDevice;
+    if (form < 0 || form > 3) return (int)cudaErrorInvalidValue;
+    Device* D = current_device();
+    if (!D) return (int)cudaErrorNoDevice;
     if (reinterpret_cast<uintptr_t>(packets) & 3u) return (int)cudaErrorMisalignedAddress;
     SigBatch b{packets, packets_len, message_lens, public_key_offsets, signature_offsets,
-               message_start_offsets, num, out, T};
-    return (int)launch_ed25519_verify_form(b, static_cast<cudaStream_t>(stream), form);
+               message_start_offsets, num, out, D->tables};
+    b.window = form == 2 ? 4 : form == 3 ? 5 : verify_window_if_tuned(*D);
+    return (int)launch_ed25519_verify_form(b, static_cast<cudaStream_t>(stream),
+                                           form == 1 ? kVerifyQuad : kVerifySingle);
 }
 
 int gb300_ed25519_sign_device(const uint8_t* packets, uint64_t packets_len, const uint32_t* message_lens,
@@ -778,11 +797,14 @@ int gb300_crypt_tuning(char* buf, size_t len) {
     const Tuning& T = tuning_for(*D);
     int n = snprintf(buf, len,
                      "{\"device\": %d, \"sms\": %d, \"sig_threads\": %d, \"sig_blocks_per_sm\": %d, "
-                     "\"sig_calibration_ms\": {\"64\": %.4f, \"128\": %.4f, \"256\": %.4f}, "
+                     "\"verify_window\": %d, "
+                     "\"sig_calibration_ms\": {\"w4\": {\"64\": %.4f, \"128\": %.4f, \"256\": %.4f}, "
+                     "\"w5\": {\"64\": %.4f, \"128\": %.4f, \"256\": %.4f}}, "
                      "\"sig_calibration_items\": %d, \"poh_warps_per_smsp\": %d, \"poh_paired\": %d, "
                      "\"poh_calibration_ms\": {\"single_1\": %.4f, \"single_2\": %.4f, \"paired_1\": %.4f, "
                      "\"paired_2\": %.4f}, \"poh_calibration_chains\": %d}",
-                     D->id, D->sms, T.sig_threads, T.sig_blocks_per_sm, T.sig_ms[0], T.sig_ms[1], T.sig_ms[2],
+                     D->id, D->sms, T.sig_threads, T.sig_blocks_per_sm, T.verify_window, T.sig_ms[0][0],
+                     T.sig_ms[0][1], T.sig_ms[0][2], T.sig_ms[1][0], T.sig_ms[1][1], T.sig_ms[1][2],
                      T.calib_sigs, T.poh_warps_per_smsp, T.poh_form == kPohPair, T.poh_ms[0], T.poh_ms[1],
                      T.poh_ms[2], T.poh_ms[3], T.calib_chains);
     return n < 0 ? 0 : (n < (int)len ? n : (int)len - 1);
@@ -882,6 +904,7 @@ int gb300_ed25519_batch_device(const uint8_t* packets, uint64_t packets_len, con
     w.sign_base = (nv + 31u) / 32u * 32u;
     w.total_chunks = (w.sign_base + ns + 31u) / 32u;
     w.next = queue_word;
+    w.v.window = T.verify_window;
     return (int)launch_sig_batch(w, T.sig_threads, T.sig_blocks_per_sm, D->sms, static_cast<cudaStream_t>(stream));
 }
 
@@ -960,9 +983,11 @@ int gb300_ed25519_batch(const gb300_sig_job* jobs, uint32_t num_jobs) {
         w.sign_base = (uint32_t)((nv + 31) / 32 * 32);
         w.total_chunks = (uint32_t)((w.sign_base + ns + 31) / 32);
         w.next = static_cast<uint32_t*>(Q.d_scratch.p);
+        w.v.window = T.verify_window;
         std::vector<uint64_t> key = {nv, ns, total, (uint64_t)(uintptr_t)dpk, (uint64_t)(uintptr_t)dv,
                                      (uint64_t)(uintptr_t)dout, (uint64_t)(uintptr_t)w.next,
-                                     (uint64_t)T.sig_threads, (uint64_t)T.sig_blocks_per_sm};
+                                     (uint64_t)T.sig_threads, (uint64_t)T.sig_blocks_per_sm,
+                                     (uint64_t)T.verify_window};
         const int sms = L.dev->sms;
         TRY(run_graph(Q.g_sig, key, s, [&](cudaStream_t cs) {
             return launch_sig_batch(w, T.sig_threads, T.sig_blocks_per_sm, sms, cs);
@@ -1024,7 +1049,7 @@ int gb300_ed25519_verify_packets_device(const uint8_t* packets, uint64_t stride,
     const Tuning& T = tuning_for(*D);
     return (int)launch_packets_verify(packets, stride, num_packets, packet_lens, workspace, workspace_bytes,
                                       packet_out, sig_counts, D->tables, T.sig_threads, T.sig_blocks_per_sm,
-                                      D->sms, static_cast<cudaStream_t>(stream));
+                                      D->sms, static_cast<cudaStream_t>(stream), T.verify_window);
 }
 
 int gb300_ed25519_verify_packets(const gpu_Elems* elems, uint32_t num_elems, uint32_t stride,
@@ -1081,10 +1106,10 @@ int gb300_ed25519_verify_packets(const gpu_Elems* elems, uint32_t num_elems, uin
         uint8_t* dout = static_cast<uint8_t*>(Q.d_out.p);
         uint32_t* dcnt = reinterpret_cast<uint32_t*>(dout + out_off);
         std::vector<uint64_t> key = {1, n, stride, (uint64_t)(uintptr_t)dpk, (uint64_t)(uintptr_t)Q.d_scratch.p,
-                                     (uint64_t)(uintptr_t)dout, (uint64_t)T.sig_threads};
+                                     (uint64_t)(uintptr_t)dout, (uint64_t)T.sig_threads, (uint64_t)T.verify_window};
         TRY(run_graph(Q.g_pkt, key, s, [&](cudaStream_t cs) {
             return launch_packets_verify(dpk, stride, n, dlens, Q.d_scratch.p, ws_bytes, dout, dcnt, L.dev->tables,
-                                         T.sig_threads, T.sig_blocks_per_sm, L.dev->sms, cs);
+                                         T.sig_threads, T.sig_blocks_per_sm, L.dev->sms, cs, T.verify_window);
         }));
         TRY(cudaMemcpyAsync(Q.h_out.p, dout, out_bytes, cudaMemcpyDeviceToHost, s));
         TRY(cudaStreamSynchronize(s));

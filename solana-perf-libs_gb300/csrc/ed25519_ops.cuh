@@ -183,6 +183,156 @@ __device__ bool verify_one(const SigBatch& a, const uint32_t* sVB, uint32_t i) {
 }
 
 
+// W-bit field of h starting at bit pos (h < 2^256, pos + W <= 256).
+__device__ __forceinline__ uint32_t bits_at(const uint32_t h[8], int pos, int W) {
+    const int w = pos >> 5, o = pos & 31;
+    uint32_t v = h[w] >> o;
+    if (o + W > 32 && w < 7) v |= h[w + 1] << (32 - o);
+    return v & ((1u << W) - 1u);
+}
+
+// Carry into each signed radix-2^W digit of h < 2^253 (bit j = carry into
+// digit j): digit_j = field_j + c_j - 2^W c_{j+1}, in [-2^(W-1), 2^(W-1)].
+template <int W>
+__device__ __forceinline__ uint64_t radixw_carries(const uint32_t h[8]) {
+    constexpr int NDIG = (253 + W - 1) / W;
+    uint64_t cin = 0;
+    uint32_t c = 0;
+#pragma unroll
+    for (int j = 0; j < NDIG; j++) {
+        cin |= (uint64_t)c << j;
+        const uint32_t v = bits_at(h, W * j, W) + c;
+        c = v >= (1u << (W - 1));
+    }
+    return cin;
+}
+
+// verify_one with a W-bit signed window for h (W = 4 is verify_one's
+// fixed-window form).  A Straus loop over bit positions: one doubling per
+// bit, the k(-A) addend at multiples of W, the basepoint addend (radix 256,
+// shared-memory table) at multiples of 8.  Same verdicts as verify_one.
+template <int W>
+__device__ bool verify_one_w(const SigBatch& a, const uint32_t* sVB, uint32_t i) {
+    constexpr int NDIG = (253 + W - 1) / W;       // digits of h
+    constexpr int NTAB = (1 << (W - 1)) + 1;      // k(-A), k = 0..2^(W-1)
+    constexpr int TOP = W * (NDIG - 1);
+    const uint64_t so = a.signature_offsets[i];
+    const uint64_t po = a.public_key_offsets[i];
+    const uint64_t mo = a.message_start_offsets[i];
+    const uint32_t m = a.message_lens[i];
+    if (so + 64 > a.packets_len || po + 32 > a.packets_len || mo + m > a.packets_len) return false;
+
+    uint32_t sig[16], pk[8];
+#pragma unroll
+    for (int k = 0; k < 16; k++) sig[k] = ld_u32_any(a.packets, so + 4 * k, a.packets_len);
+#pragma unroll
+    for (int k = 0; k < 8; k++) pk[k] = ld_u32_any(a.packets, po + 4 * k, a.packets_len);
+    if (sig[15] & 0xf0000000u) return false;               // S >= 2^252
+    if (enc_is_order4(sig) || enc_is_order4(pk)) return false;
+
+    uint64_t pre[8];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        pre[k] = ((uint64_t)bswap32(sig[2 * k]) << 32) | bswap32(sig[2 * k + 1]);
+        pre[4 + k] = ((uint64_t)bswap32(pk[2 * k]) << 32) | bswap32(pk[2 * k + 1]);
+    }
+    uint32_t hd[16], h[8];
+    sha512_prefixed(hd, pre, 8, a.packets, a.packets_len, mo, m);
+    sc_reduce512(h, hd);
+
+    const CurveConsts& K = a.tables->K;
+    fe ax, ay;
+    if (!ge_decode(ax, ay, pk, K)) return false;
+    fe_neg(ax, ax);
+
+    ge_cached tab[NTAB];
+    {
+        const fe d2 = K.d2;
+        ge_p3 P1, Pk;
+        ge_done t;
+        P1.X = ax;
+        P1.Y = ay;
+        fe_set(P1.Z, 1);
+        fe_mul(P1.T, ax, ay);
+        ge_cached_identity(tab[0]);
+        ge_p3_to_cached(tab[1], P1, d2);
+        ge_dbl(t, P1.X, P1.Y, P1.Z);
+        ge_to_p3(Pk, t);
+        ge_p3_to_cached(tab[2], Pk, d2);
+#pragma unroll 1
+        for (int k = 3; k < NTAB; k++) {
+            ge_add_cached(t, Pk, tab[1], false);
+            ge_to_p3(Pk, t);
+            ge_p3_to_cached(tab[k], Pk, d2);
+        }
+    }
+
+    uint32_t s[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) s[k] = sig[8 + k];
+    const uint64_t hc = radixw_carries<W>(h);
+    const uint32_t scar = radix256_carries(s);
+
+    ge_p3 R;
+    ge_p3_identity(R);
+#pragma unroll 1
+    for (int pos = TOP; pos >= 0; pos--) {
+        const bool addA = (pos % W) == 0, addB = (pos & 7) == 0;
+        ge_done t;
+        if (pos != TOP) {
+            ge_dbl(t, R.X, R.Y, R.Z);
+            if (!addA && !addB) {
+                ge_p2 q;
+                ge_to_p2(q, t);
+                R.X = q.X;
+                R.Y = q.Y;
+                R.Z = q.Z;
+                continue;
+            }
+            ge_to_p3(R, t);
+        }
+        if (addA) {
+            const int j = pos / W;
+            const int cj = (int)((hc >> j) & 1u);
+            const int cn = (j < NDIG - 1) ? (int)((hc >> (j + 1)) & 1u) : 0;
+            const int da = (int)bits_at(h, pos, W) + cj - (cn << W);
+            const int ua = min(da < 0 ? -da : da, NTAB - 1);
+            ge_add_cached(t, R, tab[ua], da < 0);
+            if (addB) ge_to_p3(R, t);
+        }
+        if (addB) {
+            const int k = pos >> 3;
+            const int byte = (int)((s[k >> 2] >> ((k & 3) * 8)) & 255u);
+            const int bc = (int)((scar >> k) & 1u);
+            const int bn = (k < 31) ? (int)((scar >> (k + 1)) & 1u) : 0;
+            const int db = byte + bc - 256 * bn;
+            const int ub = min(db < 0 ? -db : db, VB_ENTRIES - 1);
+            ge_niels nb;
+            load_vb(nb, sVB, ub);
+            ge_add_niels(t, R, nb, db < 0);
+        }
+        ge_p2 q;
+        ge_to_p2(q, t);
+        R.X = q.X;
+        R.Y = q.Y;
+        R.Z = q.Z;
+    }
+
+    uint32_t enc[8];
+    ge_encode_p2(enc, R.X, R.Y, R.Z);
+    uint32_t diff = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) diff |= enc[k] ^ sig[k];
+    return diff == 0;
+}
+
+// verdict of signature i with window width W (4: verify_one)
+template <int W>
+__device__ __forceinline__ bool verify_window(const SigBatch& a, const uint32_t* sVB, uint32_t i) {
+    if constexpr (W == 4) return verify_one(a, sVB, i);
+    else return verify_one_w<W>(a, sVB, i);
+}
+
 // [a]B for a < 2^255 (little-endian words), result in extended coordinates.
 __device__ void scalarmult_base(ge_p3& R, const uint32_t a[8], const CurveTables* T) {
     // signed radix-16 digits in [-8, 8]

@@ -20,6 +20,7 @@ struct SigBatch {
     uint32_t n;
     uint8_t* out;                 // verify: n verdict bytes; sign: n*64 bytes
     const CurveTables* tables;
+    int window = 4;               // verify: signed window width of h (4 or 5; the autotuner's choice)
 };
 
 // Ed25519 verify: out[i] = 1 if signature i is valid under the reference's
@@ -100,7 +101,7 @@ cudaError_t launch_packets_extract(const uint8_t* data, uint64_t stride, uint32_
 cudaError_t launch_packets_verify(const uint8_t* data, uint64_t stride, uint32_t n, const uint32_t* lens, void* ws,
                                   size_t ws_bytes, uint8_t* packet_out, uint32_t* counts_out,
                                   const CurveTables* tables, int sig_threads, int sig_blocks_per_sm, int sms,
-                                  cudaStream_t s);
+                                  cudaStream_t s, int verify_window = 4);
 
 // Per-device state the served loop (server.cu) needs from the pool
 // (crypt_api.cu): device tables and the autotuner's launch shapes.
@@ -109,6 +110,7 @@ struct CryptDeviceInfo {
     int sms;
     int sig_threads;
     int sig_blocks_per_sm;
+    int verify_window;      // window width of h in the one-lane verify
     int poh_warps;          // resident warps for the persistent PoH kernel
 };
 bool crypt_device_info(int dev, CryptDeviceInfo* out);

@@ -265,7 +265,7 @@ cudaError_t launch_packets_extract(const uint8_t* data, uint64_t stride, uint32_
 cudaError_t launch_packets_verify(const uint8_t* data, uint64_t stride, uint32_t n, const uint32_t* lens, void* ws,
                                   size_t ws_bytes, uint8_t* packet_out, uint32_t* counts_out,
                                   const CurveTables* tables, int sig_threads, int sig_blocks_per_sm, int sms,
-                                  cudaStream_t s) {
+                                  cudaStream_t s, int verify_window) {
     if (n == 0) return cudaSuccess;
     cudaError_t e = check_args(data, stride, n, lens, ws, ws_bytes);
     if (e != cudaSuccess) return e;
@@ -286,6 +286,7 @@ cudaError_t launch_packets_verify(const uint8_t* data, uint64_t stride, uint32_t
     sw.v.n = (uint32_t)cap;                     // capacity; the kernel reads the count
     sw.v.out = w.s_out;
     sw.v.tables = tables;
+    sw.v.window = verify_window;
     sw.s = sw.v;
     sw.s.n = 0;
     sw.sign_base = 0xffffffe0u;                 // no sign items

@@ -175,6 +175,7 @@ cudaError_t launch_sigs(gb300_server* sv, Slot& S) {
     uint8_t* dout = static_cast<uint8_t*>(S.d_out.p);
     SigWork w;
     w.v = SigBatch{dpk, total, dv, dv + nv, dv + 2 * nv, dv + 3 * nv, (uint32_t)nv, dout, sv->info.tables};
+    w.v.window = sv->info.verify_window;
     w.s = SigBatch{dpk, total, ds, ds + ns, ds + 2 * ns, ds + 3 * ns, (uint32_t)ns, dout + S.sig_out_off,
                    sv->info.tables};
     w.sign_base = (uint32_t)((nv + 31) / 32 * 32);

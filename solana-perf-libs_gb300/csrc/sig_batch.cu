@@ -33,7 +33,7 @@ __host__ __device__ __forceinline__ uint32_t sign_chunks(const SigWork& w) {
     return w.count_dev ? 0u : w.total_chunks - w.sign_base / 32u;
 }
 
-template <int T>
+template <int T, int W>
 __global__ void __launch_bounds__(T) sig_persistent_kernel(SigWork w) {
     __shared__ uint32_t sVB[VB_WORDS * VB_ENTRIES];
     for (int k = threadIdx.x; k < VB_WORDS * VB_ENTRIES; k += blockDim.x) sVB[k] = w.v.tables->vb[k];
@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(T) sig_persistent_kernel(SigWork w) {
                 if (i < vn && (lane & 3u) == 0) w.v.out[i] = ok ? 1 : 0;
             } else {
                 const uint32_t i = c * 32u + lane;
-                if (i < vn) w.v.out[i] = verify_one(w.v, sVB, i) ? 1 : 0;
+                if (i < vn) w.v.out[i] = verify_window<W>(w.v, sVB, i) ? 1 : 0;
             }
         } else {
             const uint32_t i = (c - vchunks) * 32u + lane;
@@ -65,10 +65,10 @@ __global__ void __launch_bounds__(T) sig_persistent_kernel(SigWork w) {
     }
 }
 
-template <int T>
+template <int T, int W>
 cudaError_t launch_t(const SigWork& w, int blocks_per_sm, int sms, cudaStream_t s) {
     int maxb = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, sig_persistent_kernel<T>, T, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, sig_persistent_kernel<T, W>, T, 0);
     if (e != cudaSuccess) return e;
     if (maxb < 1) maxb = 1;
     int b = blocks_per_sm < 1 ? maxb : (blocks_per_sm < maxb ? blocks_per_sm : maxb);
@@ -77,7 +77,7 @@ cudaError_t launch_t(const SigWork& w, int blocks_per_sm, int sms, cudaStream_t 
     uint32_t per_block = T / 32;
     if (grid * per_block > warps_needed) grid = (warps_needed + per_block - 1) / per_block;
     if (grid == 0) return cudaSuccess;
-    sig_persistent_kernel<T><<<grid, T, 0, s>>>(w);
+    sig_persistent_kernel<T, W><<<grid, T, 0, s>>>(w);
     return cudaGetLastError();
 }
 
@@ -94,10 +94,10 @@ cudaError_t launch_sig_batch(const SigWork& w_in, int threads, int blocks_per_sm
                (form == kVerifyQuad || (form != kVerifySingle && (uint64_t)w.v.n <= 64ull * (uint64_t)sms));
     cudaError_t e = cudaMemsetAsync(w.next, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
+    const bool w5 = w.v.window == 5;
     switch (threads) {
-        case 32: return launch_t<32>(w, blocks_per_sm, sms, s);
-        case 64: return launch_t<64>(w, blocks_per_sm, sms, s);
-        case 256: return launch_t<256>(w, blocks_per_sm, sms, s);
-        default: return launch_t<128>(w, blocks_per_sm, sms, s);
+        case 64: return w5 ? launch_t<64, 5>(w, blocks_per_sm, sms, s) : launch_t<64, 4>(w, blocks_per_sm, sms, s);
+        case 256: return w5 ? launch_t<256, 5>(w, blocks_per_sm, sms, s) : launch_t<256, 4>(w, blocks_per_sm, sms, s);
+        default: return w5 ? launch_t<128, 5>(w, blocks_per_sm, sms, s) : launch_t<128, 4>(w, blocks_per_sm, sms, s);
     }
 }

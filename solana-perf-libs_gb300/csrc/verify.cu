@@ -40,13 +40,14 @@ namespace {
 #include "ed25519_ops.cuh"
 #include "verify_quad.cuh"
 
+template <int W>
 __global__ void __launch_bounds__(VERIFY_THREADS, VERIFY_MIN_BLOCKS) ed25519_verify_kernel(SigBatch a) {
     __shared__ uint32_t sVB[VB_WORDS * VB_ENTRIES];
     for (int k = threadIdx.x; k < VB_WORDS * VB_ENTRIES; k += blockDim.x) sVB[k] = a.tables->vb[k];
     __syncthreads();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
-    a.out[i] = verify_one(a, sVB, i) ? 1 : 0;
+    a.out[i] = verify_window<W>(a, sVB, i) ? 1 : 0;
 }
 
 // Four lanes per signature (verify_quad.cuh): signature t / 4 on lane t % 4.
@@ -85,7 +86,8 @@ cudaError_t launch_ed25519_verify_form(const SigBatch& b, cudaStream_t s, int fo
         ed25519_verify_quad_kernel<<<blocks, VERIFY_THREADS, 0, s>>>(b);
     } else {
         const uint32_t blocks = (b.n + VERIFY_THREADS - 1) / VERIFY_THREADS;
-        ed25519_verify_kernel<<<blocks, VERIFY_THREADS, 0, s>>>(b);
+        if (b.window == 5) ed25519_verify_kernel<5><<<blocks, VERIFY_THREADS, 0, s>>>(b);
+        else ed25519_verify_kernel<4><<<blocks, VERIFY_THREADS, 0, s>>>(b);
     }
     return cudaGetLastError();
 }

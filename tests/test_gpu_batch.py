@@ -121,6 +121,8 @@ def test_sig_batch_device(lib, oracle):
 def test_tuning_report(lib):
     t = lib.tuning()
     assert t["sig_threads"] in (64, 128, 256)
+    assert t["verify_window"] in (4, 5)
+    assert set(t["sig_calibration_ms"]) == {"w4", "w5"}
     assert t["poh_warps_per_smsp"] in (1, 2)
     assert t["poh_paired"] in (0, 1)
     assert t["sms"] > 0

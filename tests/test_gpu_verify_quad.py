@@ -1,4 +1,5 @@
-"""The four-lanes-per-signature verify kernel (verify_quad.cuh) against the
+"""The verify forms -- four lanes per signature (verify_quad.cuh) and one
+lane per signature with a 4- or 5-bit window of h -- against the
 golden verdicts, the oracle and the one-thread kernel, with the cases that
 exercise its own final check (R decoded and compared projectively instead
 of encode + byte compare): R with its sign bit flipped, every non-canonical
@@ -28,11 +29,11 @@ def run_form(lib, sp, form):
 
 
 def both_forms(lib, oracle, sp):
+    """Every verify form (one lane with 4- and 5-bit windows, four lanes)
+    against the oracle."""
     exp = oracle.verify_packets(sp, nthreads())
-    single = run_form(lib, sp, lib.VERIFY_SINGLE)
-    quad = run_form(lib, sp, lib.VERIFY_QUAD)
-    assert np.array_equal(single, exp)
-    assert np.array_equal(quad, exp)
+    for form in (lib.VERIFY_SINGLE, lib.VERIFY_QUAD, lib.VERIFY_SINGLE_W4, lib.VERIFY_SINGLE_W5):
+        assert np.array_equal(run_form(lib, sp, form), exp), form
     return exp
 
 
@@ -41,7 +42,7 @@ def test_quad_golden(lib, golden_ed):
     items = [(bytes.fromhex(c["sig"]), bytes.fromhex(c["msg"]), bytes.fromhex(c["pk"])) for c in cases]
     sp = pack_items(items, gap_seed=5)
     exp = np.array([c["valid"] for c in cases], dtype=np.uint8)
-    for form in (lib.VERIFY_SINGLE, lib.VERIFY_QUAD):
+    for form in (lib.VERIFY_SINGLE, lib.VERIFY_QUAD, lib.VERIFY_SINGLE_W4, lib.VERIFY_SINGLE_W5):
         got = run_form(lib, sp, form)
         bad = [cases[i]["kind"] for i in np.nonzero(got != exp)[0]]
         assert not bad, (form, bad)
@@ -129,4 +130,4 @@ def test_verify_form_rejects_bad_form(lib):
     z = torch.zeros(4, dtype=torch.int32, device="cuda")
     out = torch.zeros(4, dtype=torch.uint8, device="cuda")
     with pytest.raises(RuntimeError):
-        lib.verify_device_form(torch.zeros(256, dtype=torch.uint8, device="cuda"), z, z, z, z, out, 2)
+        lib.verify_device_form(torch.zeros(256, dtype=torch.uint8, device="cuda"), z, z, z, z, out, 4)
