@@ -816,7 +816,8 @@ def run_ours(args):
     verify = {
         "metric": "Ed25519 verifies/s", "unit": "verifies/s",
         "config": {"workload": "ed25519_verify_many: 1024 packets [64-B sig][32-B pubkey][64-B msg], 10% bit-flipped",
-                   "signatures": VERIFY_N},
+                   "signatures": VERIFY_N,
+                   "kernel": "ed25519_verify_quad_kernel (four lanes per signature: batches up to 64 per SM)"},
         "value": v_value, "ms_per_step": k_s / vsteps * 1e3,
         "e2e": {"value": VERIFY_N * vsteps / e_s, "unit": "verifies/s",
                 "h2d_bytes_per_step": VERIFY_N * (160 + 16), "d2h_bytes_per_step": VERIFY_N,
