@@ -942,6 +942,8 @@ def run_case(case: str):
         pk = dev(sp.concatenated())
         for _ in range(3):
             lib.verify_device(pk, *arrs, out, stream.cuda_stream)
+    elif case == "sign-small":
+        bench_sign_device(lib, torch, 152 * 64, reps=2)
     elif case in ("verify-1024-single", "verify-1024-quad"):
         sp, _ = make_verify_data(lib, 1024, seed=7)
         dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
