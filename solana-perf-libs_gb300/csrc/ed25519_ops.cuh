@@ -334,7 +334,9 @@ __device__ __forceinline__ bool verify_window(const SigBatch& a, const uint32_t*
 }
 
 // [a]B for a < 2^255 (little-endian words), result in extended coordinates.
-__device__ void scalarmult_base(ge_p3& R, const uint32_t a[8], const CurveTables* T) {
+// comb: the table (j+1) 16^i B as comb[i * COMB_ENTRIES + j], in global or
+// shared memory; every entry of a window is read (constant time).
+__device__ __forceinline__ void scalarmult_base_tab(ge_p3& R, const uint32_t a[8], const ge_niels* comb) {
     // signed radix-16 digits in [-8, 8]
     int8_t e[64];
 #pragma unroll
@@ -359,7 +361,7 @@ __device__ void scalarmult_base(ge_p3& R, const uint32_t a[8], const CurveTables
         fe_set(sel.XY2d, 0);
 #pragma unroll
         for (int j = 0; j < COMB_ENTRIES; j++) {
-            const ge_niels& c = T->comb[i][j];
+            const ge_niels& c = comb[i * COMB_ENTRIES + j];
             bool take = (u == j + 1);
 #pragma unroll
             for (int w = 0; w < 8; w++) {
@@ -378,7 +380,11 @@ __device__ __forceinline__ void words_to_be64(uint64_t* out, const uint32_t* w, 
     for (int k = 0; k < nwords64; k++) out[k] = ((uint64_t)bswap32(w[2 * k]) << 32) | bswap32(w[2 * k + 1]);
 }
 
-__device__ void sign_one(const SigBatch& a, uint32_t i) {
+__device__ void scalarmult_base(ge_p3& R, const uint32_t a[8], const CurveTables* T) {
+    scalarmult_base_tab(R, a, &T->comb[0][0]);
+}
+
+__device__ __forceinline__ void sign_one_tab(const SigBatch& a, uint32_t i, const ge_niels* comb) {
     uint32_t* out = reinterpret_cast<uint32_t*>(a.out + 64ull * i);
     const uint64_t ko = a.signature_offsets[i];   // private key (64 bytes)
     const uint64_t po = a.public_key_offsets[i];
@@ -403,7 +409,7 @@ __device__ void sign_one(const SigBatch& a, uint32_t i) {
     sc_reduce512(r, hd);
 
     ge_p3 R;
-    scalarmult_base(R, r, a.tables);
+    scalarmult_base_tab(R, r, comb);
     uint32_t Renc[8];
     ge_encode_p2(Renc, R.X, R.Y, R.Z);
 
@@ -420,4 +426,6 @@ __device__ void sign_one(const SigBatch& a, uint32_t i) {
         out[8 + k] = S[k];
     }
 }
+
+__device__ void sign_one(const SigBatch& a, uint32_t i) { sign_one_tab(a, i, &a.tables->comb[0][0]); }
 

@@ -20,10 +20,19 @@ namespace {
 
 #include "ed25519_ops.cuh"
 
+// The comb table (48 KB) is staged into shared memory per block: every
+// window reads all 8 of its entries, broadcast to the warp, and from global
+// memory those reads stalled the kernel on the L1 round trip.
+constexpr size_t kCombBytes = sizeof(ge_niels) * COMB_WINDOWS * COMB_ENTRIES;
+
 __global__ void __launch_bounds__(SIGN_THREADS) ed25519_sign_kernel(SigBatch a) {
+    extern __shared__ uint4 s_comb4[];
+    const uint4* g = reinterpret_cast<const uint4*>(&a.tables->comb[0][0]);
+    for (uint32_t k = threadIdx.x; k < kCombBytes / 16; k += blockDim.x) s_comb4[k] = g[k];
+    __syncthreads();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
-    sign_one(a, i);
+    sign_one_tab(a, i, reinterpret_cast<const ge_niels*>(s_comb4));
 }
 
 // seed (32 B) -> sk = SHA-512(seed) with a clamped, pk = [a]B.
@@ -56,7 +65,7 @@ __global__ void ed25519_keypair_kernel(const uint8_t* seeds, uint8_t* pk_out, ui
 
 cudaError_t launch_ed25519_sign(const SigBatch& b, cudaStream_t s) {
     if (b.n == 0) return cudaSuccess;
-    ed25519_sign_kernel<<<(b.n + SIGN_THREADS - 1) / SIGN_THREADS, SIGN_THREADS, 0, s>>>(b);
+    ed25519_sign_kernel<<<(b.n + SIGN_THREADS - 1) / SIGN_THREADS, SIGN_THREADS, kCombBytes, s>>>(b);
     return cudaGetLastError();
 }
 
