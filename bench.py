@@ -549,7 +549,7 @@ def _pct(xs, q):
 
 
 def bench_serving(lib, levels=(0.1, 0.25, 0.5, 0.8, 1.0, 1.2), duration_s=1.0, max_requests=2500,
-                  plain_requests=120, burst_n=1000):
+                  plain_requests=120, burst_n=1000, server_kwargs=None):
     """Open-loop Poisson arrivals of a request mix (80% verify batches of the
     ragged-batch size/message/adversarial distributions, 15% PoH batches of
     64 entries with num_hashes log-uniform in 1..1e6, 5% sign batches of 128
@@ -602,7 +602,7 @@ def bench_serving(lib, levels=(0.1, 0.25, 0.5, 0.8, 1.0, 1.2), duration_s=1.0, m
         exp = alone_v[k] if kind == "v" else alone_s[k] if kind == "s" else alone_p[k]
         return np.array_equal(out, exp)
 
-    srv = Server(lib)
+    srv = Server(lib, **(server_kwargs or {}))
     ok_all = True
     try:
         # peak: a burst of the mix, time until its signature requests are done
