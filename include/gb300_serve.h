@@ -33,7 +33,8 @@ typedef struct {
     uint64_t device_memory_cap;      /* bytes in flight on the GPU; 0 = 8 GiB */
     uint32_t sig_slots;              /* concurrent signature launches; 0 = 3 */
     uint32_t poh_slots;              /* concurrent PoH launches; 0 = 2 */
-    uint32_t max_items_per_launch;   /* signatures merged into one launch; 0 = 65536 */
+    uint32_t max_items_per_launch;   /* signatures merged into one launch; 0 = 65536
+                                        (a larger request runs alone) */
 } gb300_server_config;
 
 /* Creates a server on the current device (cfg may be NULL); NULL on failure. */

@@ -1,7 +1,8 @@
 """The served request loop: requests submitted together (from several
 threads, mixed verify / sign / PoH) each get exactly the result they get
 alone through the one-call entry points; memory-capped admission still
-completes everything; oversize requests are refused."""
+completes everything; requests above the memory budget are refused, requests
+above the per-launch item cap run alone."""
 import threading
 
 import numpy as np
@@ -101,5 +102,22 @@ def test_merging_under_backlog(lib, mix):
             assert srv.wait(t, 60000) == 1
         st = srv.stats()
         assert st["max_requests_merged"] > 1 and st["launches_sig"] < len(sub)
+    finally:
+        srv.close()
+
+
+def test_request_above_item_cap_runs_alone(lib, mix):
+    """A request with more signatures than max_items_per_launch is not
+    refused: it runs in a launch of its own, beside merged small ones."""
+    rs, _ = mix
+    ver = [lib.verify_many(sp) for sp in rs.verify]
+    big = max(range(len(rs.verify)), key=lambda k: rs.verify[k].total_signatures)
+    cap = max(1, rs.verify[big].total_signatures // 3)
+    srv = Server(lib, max_items_per_launch=cap, sig_slots=2)
+    try:
+        sub = [(k,) + tuple(srv.submit_sigs(sp, JOB_VERIFY)) for k, sp in enumerate(rs.verify * 2)]
+        for k, t, out in sub:
+            assert t and srv.wait(t, 60000) == 1
+            assert np.array_equal(out, ver[k % len(rs.verify)])
     finally:
         srv.close()
