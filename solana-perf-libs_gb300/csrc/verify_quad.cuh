@@ -33,18 +33,21 @@
 
 constexpr uint32_t kQuadAll = 0xffffffffu;
 
-// per-lane selection masks: sel[k] = all ones on lane k of the quad
+// per-lane selection masks: lo = all ones on lanes 1 and 3 of the quad,
+// hi = all ones on lanes 2 and 3, m3 = all ones on lane 3
 struct QuadSel {
-    uint32_t m0, m1, m2, m3;
+    uint32_t lo, hi, m3;
 };
 __device__ __forceinline__ QuadSel quad_sel(uint32_t q) {
     QuadSel s;
-    s.m0 = 0u - (uint32_t)(q == 0);
-    s.m1 = 0u - (uint32_t)(q == 1);
-    s.m2 = 0u - (uint32_t)(q == 2);
-    s.m3 = 0u - (uint32_t)(q == 3);
+    s.lo = 0u - (q & 1u);
+    s.hi = 0u - ((q >> 1) & 1u);
+    s.m3 = s.lo & s.hi;
     return s;
 }
+
+// msk ? b : a per bit (one three-input logic op)
+__device__ __forceinline__ uint32_t bsel(uint32_t a, uint32_t b, uint32_t msk) { return (b & msk) | (a & ~msk); }
 
 __device__ __forceinline__ void quad_gather4(const fe& m, fe& o0, fe& o1, fe& o2, fe& o3, uint32_t mask) {
 #pragma unroll
@@ -78,12 +81,11 @@ __device__ __forceinline__ void fe_select_m(fe& r, const fe& a, const fe& b, uin
     for (int w = 0; w < 8; w++) r.v[w] = (b.v[w] & msk) | (a.v[w] & ~msk);
 }
 
-// r = (a0, a1, a2, a3)[q], branch-free
+// r = (a0, a1, a2, a3)[q], branch-free: a two-level select tree
 __device__ __forceinline__ void fe_pick4(fe& r, const fe& a0, const fe& a1, const fe& a2, const fe& a3,
                                          const QuadSel& q) {
 #pragma unroll
-    for (int w = 0; w < 8; w++)
-        r.v[w] = (a0.v[w] & q.m0) | (a1.v[w] & q.m1) | (a2.v[w] & q.m2) | (a3.v[w] & q.m3);
+    for (int w = 0; w < 8; w++) r.v[w] = bsel(bsel(a0.v[w], a1.v[w], q.lo), bsel(a2.v[w], a3.v[w], q.lo), q.hi);
 }
 
 // Doubling, first stage (four squarings), all lanes get (E, F, G, H).
