@@ -66,7 +66,10 @@ int gb300_server_times(gb300_server* s, uint64_t ticket, int64_t* submit_ns, int
 
 /* Timeline of the most recent launches as a JSON array of
  * [kind (0 signatures, 2 PoH), requests merged, items, admitted_ns,
- *  enqueued_ns, completed_ns]; returns the length written. */
+ *  enqueued_ns, completed_ns, copy_in_ms, kernels_ms, copy_out_ms]: host
+ * times of the launch, then the GPU time of its input copies, its kernels
+ * and its result copy (CUDA events; -1 after a failure); returns the
+ * length written. */
 int gb300_server_trace(gb300_server* s, char* buf, size_t len);
 
 /* Counters as a JSON object; returns the length written. */

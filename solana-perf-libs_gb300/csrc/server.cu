@@ -64,6 +64,9 @@ struct Slot {
     int64_t t_admit = 0, t_enqueued = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
+    // timed GPU phases of the launch: ev_in (inputs start copying), ev_run
+    // (kernels start), ev_out (results start copying), done (all copied)
+    cudaEvent_t ev_in = nullptr, ev_run = nullptr, ev_out = nullptr;
     bool busy = false;
     int kind = 0;                 // 0 signatures, 2 PoH
     DevBuf d_data, d_index, d_out, d_scratch;
@@ -100,6 +103,7 @@ struct gb300_server {
         uint32_t reqs;
         uint64_t items;
         int64_t t_admit, t_enqueued, t_complete;
+        float copy_in_ms, kernels_ms, copy_out_ms;   // GPU time of each phase (events)
     };
     std::vector<Trace> trace;
 };
@@ -141,6 +145,7 @@ cudaError_t launch_sigs(gb300_server* sv, Slot& S) {
     uint8_t* img = static_cast<uint8_t*>(S.h_stage.p) + pk_off;
     uint8_t* dpk = static_cast<uint8_t*>(S.d_data.p);
     uint64_t base = 0, iv = 0, is = 0;
+    if ((e = cudaEventRecord(S.ev_in, S.stream)) != cudaSuccess) return e;
     for (auto& r : S.reqs) {
         const gb300_sig_job& J = r.job;
         uint32_t* h = r.kind == 0 ? hv : hs;
@@ -181,9 +186,11 @@ cudaError_t launch_sigs(gb300_server* sv, Slot& S) {
     w.sign_base = (uint32_t)((nv + 31) / 32 * 32);
     w.total_chunks = (uint32_t)((w.sign_base + ns + 31) / 32);
     w.next = static_cast<uint32_t*>(S.d_scratch.p);
+    if ((e = cudaEventRecord(S.ev_run, S.stream)) != cudaSuccess) return e;
     if ((e = launch_sig_batch(w, sv->info.sig_threads, sv->info.sig_blocks_per_sm, sv->info.sms, S.stream)) !=
         cudaSuccess)
         return e;
+    if ((e = cudaEventRecord(S.ev_out, S.stream)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(S.h_out.p, dout, out_bytes, cudaMemcpyDeviceToHost, S.stream)) != cudaSuccess) return e;
     return cudaEventRecord(S.done, S.stream);
 }
@@ -205,10 +212,13 @@ cudaError_t launch_pohs(gb300_server* sv, Slot& S) {
         pos += r.n;
     }
     uint8_t* d = static_cast<uint8_t*>(S.d_data.p);
+    if ((e = cudaEventRecord(S.ev_in, S.stream)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(d, st, hb + cb, cudaMemcpyHostToDevice, S.stream)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(S.ev_run, S.stream)) != cudaSuccess) return e;
     if ((e = launch_poh_batch(d, reinterpret_cast<const uint64_t*>(d + hb), n, S.d_scratch.p, sv->poh_warps,
                               S.stream, sv->poh_form)) != cudaSuccess)
         return e;
+    if ((e = cudaEventRecord(S.ev_out, S.stream)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(st, d, hb, cudaMemcpyDeviceToHost, S.stream)) != cudaSuccess) return e;
     return cudaEventRecord(S.done, S.stream);
 }
@@ -266,7 +276,15 @@ void dispatcher(gb300_server* sv) {
                     uint64_t it = 0;
                     for (auto& r : S.reqs) it += r.n;
                     if (sv->trace.size() >= 4096) sv->trace.erase(sv->trace.begin(), sv->trace.begin() + 1024);
-                    sv->trace.push_back({S.kind, (uint32_t)S.reqs.size(), it, S.t_admit, S.t_enqueued, t_done});
+                    float ms_in = -1.f, ms_run = -1.f, ms_out = -1.f;
+                    if (S.err == cudaSuccess) {
+                        if (cudaEventElapsedTime(&ms_in, S.ev_in, S.ev_run) != cudaSuccess) ms_in = -1.f;
+                        if (cudaEventElapsedTime(&ms_run, S.ev_run, S.ev_out) != cudaSuccess) ms_run = -1.f;
+                        if (cudaEventElapsedTime(&ms_out, S.ev_out, S.done) != cudaSuccess) ms_out = -1.f;
+                        cudaGetLastError();
+                    }
+                    sv->trace.push_back({S.kind, (uint32_t)S.reqs.size(), it, S.t_admit, S.t_enqueued, t_done, ms_in,
+                                         ms_run, ms_out});
                 }
                 for (auto& r : S.reqs) {
                     sv->times[r.ticket].second = t_done;
@@ -394,10 +412,12 @@ gb300_server* gb300_server_create(const gb300_server_config* cfg) {
     bool ok = true;
     for (auto& S : sv->sig_slots)
         ok = ok && cudaStreamCreateWithPriority(&S.stream, cudaStreamNonBlocking, hi) == cudaSuccess &&
-             cudaEventCreateWithFlags(&S.done, cudaEventDisableTiming) == cudaSuccess;
+             cudaEventCreate(&S.done) == cudaSuccess && cudaEventCreate(&S.ev_in) == cudaSuccess &&
+             cudaEventCreate(&S.ev_run) == cudaSuccess && cudaEventCreate(&S.ev_out) == cudaSuccess;
     for (auto& S : sv->poh_slots)
         ok = ok && cudaStreamCreateWithPriority(&S.stream, cudaStreamNonBlocking, lo) == cudaSuccess &&
-             cudaEventCreateWithFlags(&S.done, cudaEventDisableTiming) == cudaSuccess;
+             cudaEventCreate(&S.done) == cudaSuccess && cudaEventCreate(&S.ev_in) == cudaSuccess &&
+             cudaEventCreate(&S.ev_run) == cudaSuccess && cudaEventCreate(&S.ev_out) == cudaSuccess;
     // resident rings: each signature slot holds a 64 MiB packet ring and the
     // index/output space of a full launch; each PoH slot 65536 entries
     for (auto& S : sv->sig_slots) {
@@ -444,7 +464,8 @@ void gb300_server_destroy(gb300_server* sv) {
             S.d_scratch.release();
             S.h_stage.release();
             S.h_out.release();
-            if (S.done) cudaEventDestroy(S.done);
+            for (cudaEvent_t ev : {S.done, S.ev_in, S.ev_run, S.ev_out})
+                if (ev) cudaEventDestroy(ev);
             if (S.stream) cudaStreamDestroy(S.stream);
         }
     if (prev >= 0) cudaSetDevice(prev);
@@ -540,9 +561,9 @@ int gb300_server_trace(gb300_server* sv, char* buf, size_t len) {
     off = (size_t)n;
     for (size_t i = 0; i < sv->trace.size() && off + 128 < len; i++) {
         const auto& t = sv->trace[i];
-        n = snprintf(buf + off, len - off, "%s[%d,%u,%llu,%lld,%lld,%lld]", i ? "," : "", t.kind, t.reqs,
-                     (unsigned long long)t.items, (long long)t.t_admit, (long long)t.t_enqueued,
-                     (long long)t.t_complete);
+        n = snprintf(buf + off, len - off, "%s[%d,%u,%llu,%lld,%lld,%lld,%.4f,%.4f,%.4f]", i ? "," : "", t.kind,
+                     t.reqs, (unsigned long long)t.items, (long long)t.t_admit, (long long)t.t_enqueued,
+                     (long long)t.t_complete, t.copy_in_ms, t.kernels_ms, t.copy_out_ms);
         if (n < 0) break;
         off += (size_t)n;
     }
