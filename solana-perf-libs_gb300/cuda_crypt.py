@@ -467,6 +467,16 @@ class Server:
         n = self.L.gb300_server_stats(self.h, buf, 1024)
         return json.loads(buf.value[:n].decode()) if n else {}
 
+    def trace(self) -> list:
+        """Recent launches: [kind, requests, items, admitted_ns, enqueued_ns,
+        completed_ns, copy_in_ms, kernels_ms, copy_out_ms] each."""
+        import json
+        self.L.gb300_server_trace.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]
+        self.L.gb300_server_trace.restype = ctypes.c_int
+        buf = ctypes.create_string_buffer(1 << 22)
+        n = self.L.gb300_server_trace(self.h, buf, len(buf))
+        return json.loads(buf.value[:n].decode()) if n else []
+
     def close(self) -> None:
         if self.h:
             self.L.gb300_server_destroy(self.h)

@@ -121,3 +121,24 @@ def test_request_above_item_cap_runs_alone(lib, mix):
             assert np.array_equal(out, ver[k % len(rs.verify)])
     finally:
         srv.close()
+
+
+def test_trace_records_gpu_phases(lib, mix):
+    """Every completed launch appears in the trace with its host times and
+    the GPU time of its copies and kernels."""
+    rs, pohs = mix
+    srv = Server(lib)
+    try:
+        subs = [srv.submit_sigs(sp, JOB_VERIFY)[0] for sp in rs.verify]
+        h, c = pohs[0]
+        subs.append(srv.submit_poh(h.ravel().copy(), c))
+        for t in subs:
+            assert srv.wait(t, 60000) == 1
+        tr = srv.trace()
+        assert len(tr) >= 2 and {e[0] for e in tr} == {0, 2}
+        for kind, reqs, items, t_admit, t_enq, t_done, ms_in, ms_run, ms_out in tr:
+            assert reqs >= 1 and items >= 1 and t_admit <= t_enq <= t_done
+            assert ms_in >= 0 and ms_run > 0 and ms_out >= 0
+        assert sum(e[1] for e in tr) == len(subs)
+    finally:
+        srv.close()
