@@ -13,6 +13,7 @@
 //     chunks (early rejections, short messages) simply takes more;
 //   * each block stages the verify basepoint table into shared memory once.
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cstdlib>
 #include "kernels.h"
 #include "tables.cuh"
@@ -33,10 +34,21 @@ __host__ __device__ __forceinline__ uint32_t sign_chunks(const SigWork& w) {
     return w.count_dev ? 0u : w.total_chunks - w.sign_base / 32u;
 }
 
+// Launches with sign items also stage the signing comb (48 KB) into dynamic
+// shared memory: each sign reads all 8 entries of 64 windows, and from
+// global memory those reads stall on the L1 round trip.
+constexpr size_t kCombBytes = sizeof(ge_niels) * COMB_WINDOWS * COMB_ENTRIES;
+
 template <int T, int W>
 __global__ void __launch_bounds__(T) sig_persistent_kernel(SigWork w) {
     __shared__ uint32_t sVB[VB_WORDS * VB_ENTRIES];
+    extern __shared__ uint4 s_comb4[];
     for (int k = threadIdx.x; k < VB_WORDS * VB_ENTRIES; k += blockDim.x) sVB[k] = w.v.tables->vb[k];
+    const bool comb_in_smem = w.s.n > 0;          // launch-uniform: dynamic size is kCombBytes then
+    if (comb_in_smem) {
+        const uint4* g = reinterpret_cast<const uint4*>(&w.s.tables->comb[0][0]);
+        for (uint32_t k = threadIdx.x; k < kCombBytes / 16; k += blockDim.x) s_comb4[k] = g[k];
+    }
     __syncthreads();
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t vn = w.count_dev ? *w.count_dev : w.v.n;
@@ -60,15 +72,30 @@ __global__ void __launch_bounds__(T) sig_persistent_kernel(SigWork w) {
             }
         } else {
             const uint32_t i = (c - vchunks) * 32u + lane;
-            if (i < w.s.n) sign_one(w.s, i);
+            if (i < w.s.n) sign_one_tab(w.s, i, reinterpret_cast<const ge_niels*>(s_comb4));
         }
     }
 }
 
 template <int T, int W>
 cudaError_t launch_t(const SigWork& w, int blocks_per_sm, int sms, cudaStream_t s) {
+    // 12 KB static + 48 KB dynamic shared memory is above the 48 KB a block
+    // gets without opting in; the opt-in is an attribute of the function on
+    // each device, set on the device's first launch
+    static std::atomic<uint64_t> opted{0};      // bit d: done on device d
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const uint64_t bit = 1ull << (dev & 63);
+    if (!(opted.load() & bit)) {
+        e = cudaFuncSetAttribute(sig_persistent_kernel<T, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kCombBytes);
+        if (e != cudaSuccess) return e;
+        opted.fetch_or(bit);
+    }
+    const size_t dyn = w.s.n > 0 ? kCombBytes : 0;
     int maxb = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, sig_persistent_kernel<T, W>, T, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, sig_persistent_kernel<T, W>, T, dyn);
     if (e != cudaSuccess) return e;
     if (maxb < 1) maxb = 1;
     int b = blocks_per_sm < 1 ? maxb : (blocks_per_sm < maxb ? blocks_per_sm : maxb);
@@ -77,7 +104,7 @@ cudaError_t launch_t(const SigWork& w, int blocks_per_sm, int sms, cudaStream_t 
     uint32_t per_block = T / 32;
     if (grid * per_block > warps_needed) grid = (warps_needed + per_block - 1) / per_block;
     if (grid == 0) return cudaSuccess;
-    sig_persistent_kernel<T, W><<<grid, T, 0, s>>>(w);
+    sig_persistent_kernel<T, W><<<grid, T, dyn, s>>>(w);
     return cudaGetLastError();
 }
 
