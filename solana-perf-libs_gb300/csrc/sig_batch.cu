@@ -28,7 +28,8 @@ namespace {
 // Chunk counts of a launch: verify chunks (32 signatures, or 8 in quad
 // mode), then sign chunks of 32.
 __host__ __device__ __forceinline__ uint32_t verify_chunks(const SigWork& w, uint32_t vn) {
-    return w.count_dev ? (vn + 31u) / 32u : w.v_quad ? (vn + 7u) / 8u : w.sign_base / 32u;
+    if (w.v_quad) return (vn + 7u) / 8u;
+    return w.count_dev ? (vn + 31u) / 32u : w.sign_base / 32u;
 }
 __host__ __device__ __forceinline__ uint32_t sign_chunks(const SigWork& w) {
     return w.count_dev ? 0u : w.total_chunks - w.sign_base / 32u;
@@ -117,7 +118,8 @@ cudaError_t launch_sig_batch(const SigWork& w_in, int threads, int blocks_per_sm
     SigWork w = w_in;
     static const int forced = getenv("GB300_CRYPT_VERIFY_FORM") ? atoi(getenv("GB300_CRYPT_VERIFY_FORM")) : -1;
     const int form = (forced == kVerifySingle || forced == kVerifyQuad) ? forced : w.v_form_hint;
-    w.v_quad = !w.count_dev && w.v.n > 0 &&
+    // (with a device count, v.n is the capacity: the rule then uses the bound)
+    w.v_quad = w.v.n > 0 &&
                (form == kVerifyQuad || (form != kVerifySingle && (uint64_t)w.v.n <= 64ull * (uint64_t)sms));
     cudaError_t e = cudaMemsetAsync(w.next, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
