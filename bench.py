@@ -961,6 +961,28 @@ def run_case(case: str):
         pk = dev(sp.concatenated())
         for _ in range(3):   # the one-lane kernel (9,728 would pick the four-lane form by size)
             lib.verify_device_form(pk, *arrs, out, lib.VERIFY_SINGLE_W4, stream.cuda_stream)
+    elif case == "ragged-batch-small":
+        # ragged verify jobs + 128-packet sign jobs in one persistent launch, device-resident
+        rs = workloads.ragged_sigs(lib.create_keypairs, lib.sign_many, n_batches=12, seed=3)
+        pk_parts, v_idx, s_idx, base = [], [[], [], [], []], [[], [], [], []], 0
+        for group, idx in ((rs.verify, v_idx), (rs.sign, s_idx)):
+            for sp in group:
+                c = sp.concatenated()
+                pk_parts.append(c)
+                for k, a in enumerate((sp.message_lens, sp.public_key_offsets + base, sp.signature_offsets + base,
+                                       sp.message_start_offsets + base)):
+                    idx[k].append(np.asarray(a, dtype=np.int64))
+                base += len(c)
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        packets = dev(np.concatenate(pk_parts))
+        v = [dev(np.concatenate(x).astype(np.int32)) for x in v_idx]
+        s_ = [dev(np.concatenate(x).astype(np.int32)) for x in s_idx]
+        v_out = torch.zeros(v[0].numel(), dtype=torch.uint8, device="cuda")
+        s_out = torch.zeros((s_[0].numel(), 64), dtype=torch.uint8, device="cuda")
+        q = torch.zeros(4, dtype=torch.int32, device="cuda")
+        for _ in range(3):
+            lib.ed25519_batch_device(packets, v, v_out, s_, s_out, q, stream.cuda_stream)
+        print("items", v[0].numel(), s_[0].numel())
     elif case == "sign-small":
         bench_sign_device(lib, torch, 152 * 64, reps=2)
     elif case in ("verify-1024-single", "verify-1024-quad"):
