@@ -983,6 +983,15 @@ def run_case(case: str):
         for _ in range(3):
             lib.ed25519_batch_device(packets, v, v_out, s_, s_out, q, stream.cuda_stream)
         print("items", v[0].numel(), s_[0].numel())
+    elif case == "verify-big":
+        sp, _ = make_verify_data(lib, VERIFY_BIG_N, seed=5)
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        arrs = [dev(a.astype(np.int32)) for a in
+                (sp.message_lens, sp.public_key_offsets, sp.signature_offsets, sp.message_start_offsets)]
+        out = torch.zeros(sp.total_signatures, dtype=torch.uint8, device="cuda")
+        pk = dev(sp.concatenated())
+        for _ in range(2):
+            lib.verify_device_form(pk, *arrs, out, lib.VERIFY_SINGLE_W4, stream.cuda_stream)
     elif case == "sign-small":
         bench_sign_device(lib, torch, 152 * 64, reps=2)
     elif case in ("verify-1024-single", "verify-1024-quad"):
