@@ -40,8 +40,13 @@ namespace {
 #include "ed25519_ops.cuh"
 #include "verify_quad.cuh"
 
-template <int W>
-__global__ void __launch_bounds__(VERIFY_THREADS, VERIFY_MIN_BLOCKS) ed25519_verify_kernel(SigBatch a) {
+// MINB: blocks per SM the register allocation must allow.  1 lets the
+// compiler keep everything in registers (254; 2 blocks of 128 fit); 4 caps
+// it at 128 registers, with some spills, for batches large enough to fill
+// 4 blocks per SM, where the extra warps hide more latency (measured at
+// 116,736 signatures: 4.27 ms against 4.57; at 32,768 it is 4 % slower).
+template <int W, int MINB>
+__global__ void __launch_bounds__(VERIFY_THREADS, MINB) ed25519_verify_kernel(SigBatch a) {
     __shared__ uint32_t sVB[VB_WORDS * VB_ENTRIES];
     for (int k = threadIdx.x; k < VB_WORDS * VB_ENTRIES; k += blockDim.x) sVB[k] = a.tables->vb[k];
     __syncthreads();
@@ -86,8 +91,18 @@ cudaError_t launch_ed25519_verify_form(const SigBatch& b, cudaStream_t s, int fo
         ed25519_verify_quad_kernel<<<blocks, VERIFY_THREADS, 0, s>>>(b);
     } else {
         const uint32_t blocks = (b.n + VERIFY_THREADS - 1) / VERIFY_THREADS;
-        if (b.window == 5) ed25519_verify_kernel<5><<<blocks, VERIFY_THREADS, 0, s>>>(b);
-        else ed25519_verify_kernel<4><<<blocks, VERIFY_THREADS, 0, s>>>(b);
+        if (b.window == 5) {
+            ed25519_verify_kernel<5, VERIFY_MIN_BLOCKS><<<blocks, VERIFY_THREADS, 0, s>>>(b);
+        } else {
+            int dev = 0, sms = 0;
+            if (cudaGetDevice(&dev) != cudaSuccess ||
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+                return cudaGetLastError();
+            if ((uint64_t)b.n >= 4ull * VERIFY_THREADS * (uint64_t)sms)
+                ed25519_verify_kernel<4, 4><<<blocks, VERIFY_THREADS, 0, s>>>(b);
+            else
+                ed25519_verify_kernel<4, VERIFY_MIN_BLOCKS><<<blocks, VERIFY_THREADS, 0, s>>>(b);
+        }
     }
     return cudaGetLastError();
 }
