@@ -14,7 +14,17 @@
 #include "sha512.cuh"
 #include "sc25519.cuh"
 
+#ifndef SIGN_THREADS
 #define SIGN_THREADS 128
+#endif
+#ifndef SIGN_MIN_BLOCKS
+#define SIGN_MIN_BLOCKS 0   // 0: no minimum in the launch bounds
+#endif
+#if SIGN_MIN_BLOCKS > 0
+#define SIGN_BOUNDS __launch_bounds__(SIGN_THREADS, SIGN_MIN_BLOCKS)
+#else
+#define SIGN_BOUNDS __launch_bounds__(SIGN_THREADS)
+#endif
 
 namespace {
 
@@ -25,7 +35,7 @@ namespace {
 // memory those reads stalled the kernel on the L1 round trip.
 constexpr size_t kCombBytes = sizeof(ge_niels) * COMB_WINDOWS * COMB_ENTRIES;
 
-__global__ void __launch_bounds__(SIGN_THREADS) ed25519_sign_kernel(SigBatch a) {
+__global__ void SIGN_BOUNDS ed25519_sign_kernel(SigBatch a) {
     extern __shared__ uint4 s_comb4[];
     const uint4* g = reinterpret_cast<const uint4*>(&a.tables->comb[0][0]);
     for (uint32_t k = threadIdx.x; k < kCombBytes / 16; k += blockDim.x) s_comb4[k] = g[k];
