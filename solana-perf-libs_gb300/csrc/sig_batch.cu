@@ -40,8 +40,10 @@ __host__ __device__ __forceinline__ uint32_t sign_chunks(const SigWork& w) {
 // global memory those reads stall on the L1 round trip.
 constexpr size_t kCombBytes = sizeof(ge_niels) * COMB_WINDOWS * COMB_ENTRIES;
 
-template <int T, int W>
-__global__ void __launch_bounds__(T) sig_persistent_kernel(SigWork w) {
+// MINB > 0: the build capped for MINB blocks per SM (more warps to hide the
+// dependent carry chains, some spills), used for launches that fill them.
+template <int T, int W, int MINB>
+__global__ void __launch_bounds__(T, MINB) sig_persistent_kernel(SigWork w) {
     __shared__ uint32_t sVB[VB_WORDS * VB_ENTRIES];
     extern __shared__ uint4 s_comb4[];
     for (int k = threadIdx.x; k < VB_WORDS * VB_ENTRIES; k += blockDim.x) sVB[k] = w.v.tables->vb[k];
@@ -78,7 +80,7 @@ __global__ void __launch_bounds__(T) sig_persistent_kernel(SigWork w) {
     }
 }
 
-template <int T, int W>
+template <int T, int W, int MINB>
 cudaError_t launch_t(const SigWork& w, int blocks_per_sm, int sms, cudaStream_t s) {
     // 12 KB static + 48 KB dynamic shared memory is above the 48 KB a block
     // gets without opting in; the opt-in is an attribute of the function on
@@ -89,14 +91,14 @@ cudaError_t launch_t(const SigWork& w, int blocks_per_sm, int sms, cudaStream_t 
     if (e != cudaSuccess) return e;
     const uint64_t bit = 1ull << (dev & 63);
     if (!(opted.load() & bit)) {
-        e = cudaFuncSetAttribute(sig_persistent_kernel<T, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(sig_persistent_kernel<T, W, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)kCombBytes);
         if (e != cudaSuccess) return e;
         opted.fetch_or(bit);
     }
     const size_t dyn = w.s.n > 0 ? kCombBytes : 0;
     int maxb = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, sig_persistent_kernel<T, W>, T, dyn);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, sig_persistent_kernel<T, W, MINB>, T, dyn);
     if (e != cudaSuccess) return e;
     if (maxb < 1) maxb = 1;
     int b = blocks_per_sm < 1 ? maxb : (blocks_per_sm < maxb ? blocks_per_sm : maxb);
@@ -105,7 +107,7 @@ cudaError_t launch_t(const SigWork& w, int blocks_per_sm, int sms, cudaStream_t 
     uint32_t per_block = T / 32;
     if (grid * per_block > warps_needed) grid = (warps_needed + per_block - 1) / per_block;
     if (grid == 0) return cudaSuccess;
-    sig_persistent_kernel<T, W><<<grid, T, dyn, s>>>(w);
+    sig_persistent_kernel<T, W, MINB><<<grid, T, dyn, s>>>(w);
     return cudaGetLastError();
 }
 
@@ -124,9 +126,16 @@ cudaError_t launch_sig_batch(const SigWork& w_in, int threads, int blocks_per_sm
     cudaError_t e = cudaMemsetAsync(w.next, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     const bool w5 = w.v.window == 5;
+    // a launch with chunks for 3 blocks of 128 threads on every SM runs the
+    // build capped at 3 blocks per SM (1 minimum otherwise)
+    const uint64_t warps = (uint64_t)verify_chunks(w, w.v.n) + sign_chunks(w);
+    const bool full = threads != 64 && threads != 256 && !w5 && blocks_per_sm < 1 && warps >= 12ull * (uint64_t)sms;
     switch (threads) {
-        case 64: return w5 ? launch_t<64, 5>(w, blocks_per_sm, sms, s) : launch_t<64, 4>(w, blocks_per_sm, sms, s);
-        case 256: return w5 ? launch_t<256, 5>(w, blocks_per_sm, sms, s) : launch_t<256, 4>(w, blocks_per_sm, sms, s);
-        default: return w5 ? launch_t<128, 5>(w, blocks_per_sm, sms, s) : launch_t<128, 4>(w, blocks_per_sm, sms, s);
+        case 64: return w5 ? launch_t<64, 5, 1>(w, blocks_per_sm, sms, s) : launch_t<64, 4, 1>(w, blocks_per_sm, sms, s);
+        case 256:
+            return w5 ? launch_t<256, 5, 1>(w, blocks_per_sm, sms, s) : launch_t<256, 4, 1>(w, blocks_per_sm, sms, s);
+        default:
+            if (full) return launch_t<128, 4, 3>(w, blocks_per_sm, sms, s);
+            return w5 ? launch_t<128, 5, 1>(w, blocks_per_sm, sms, s) : launch_t<128, 4, 1>(w, blocks_per_sm, sms, s);
     }
 }
