@@ -536,6 +536,7 @@ def bench_wire_packets(lib, torch, nthreads, n=16384, reps=5):
     bad = np.zeros(n, dtype=np.int64)
     np.add.at(bad, pkt, (per_sig == 0).astype(np.int64))
     same = bool(np.array_equal(((c2 > 0) & (bad == 0)).astype(np.uint8), out) and np.array_equal(c2, counts))
+    served = _served_packets(lib, w, out, counts)
     lib.host_unregister(w.data)
     # CPU baseline: the oracle parses and verifies the whole batch on all host cores
     t = time.perf_counter()
@@ -554,9 +555,103 @@ def bench_wire_packets(lib, torch, nthreads, n=16384, reps=5):
                                             "value": n / (parse_s + offsets_e2e_s), "unit": "packets/s",
                                             "h2d_bytes_per_step": n * stride + 16 * nsig,
                                             "parse": "oracle C parse on 1 host thread (the caller's work)"},
-            "results_identical_device_parse_vs_host_parse": same,
+            "results_identical_device_parse_vs_host_parse": same, "served": served,
             "cpu_baseline": {"value": n / cpu_s, "unit": "packets/s", "cores": nthreads, "kind": "port",
                              "sample": f"the full batch ({nsig} signatures), CPU oracle parse + verify"}}
+
+
+def _served_packets(lib, w, out, counts, batch=128, levels=(0.25, 0.5, 0.8), max_requests=4000, reps=3):
+    """The same packets as a stream of `batch`-packet batches (views of the
+    page-locked buffer) through the served loop
+    (gb300_server_submit_packets): the peak as a burst of every batch timed
+    to the last completion, then open-loop Poisson arrivals at fractions of
+    it; against one caller handing each batch to
+    gb300_ed25519_verify_packets in turn.  Submissions go through one raw
+    ctypes call with arguments prepared beforehand, so that the Python
+    submitter keeps up with the offered rate.  Every result is checked
+    against the whole-batch verdicts."""
+    import ctypes
+    from cuda_crypt import GpuElems, Server
+    nb = len(w.lens) // batch
+    stride = w.stride
+    views = [(w.data[k * batch:(k + 1) * batch], w.lens[k * batch:(k + 1) * batch]) for k in range(nb)]
+    runs = []
+    for d, _ in views:
+        e = (GpuElems * 1)()
+        e[0].elems = d.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+        e[0].num = batch
+        runs.append(e)
+    run_addr = [ctypes.addressof(e) for e in runs]
+    lens_addr = [ln.ctypes.data for _, ln in views]
+    submit = lib.lib["gb300_server_submit_packets"]
+    submit.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p,
+                       ctypes.c_void_p, ctypes.c_void_p]
+    submit.restype = ctypes.c_uint64
+
+    def outputs(m):
+        o = np.zeros((m, batch), dtype=np.uint8)
+        c = np.zeros((m, batch), dtype=np.uint32)
+        return o, c, o.ctypes.data, c.ctypes.data
+
+    def same(k, o, c):
+        return np.array_equal(o, out[k * batch:(k + 1) * batch]) and np.array_equal(c, counts[k * batch:(k + 1) * batch])
+
+    ok = True
+    rng = np.random.default_rng(21)
+    srv = Server(lib)
+    try:
+        bursts = []
+        for rep in range(reps + 1):                   # the first burst warms the server up
+            o, c, ob, cb = outputs(nb)
+            t0 = time.perf_counter()
+            tk = [submit(srv.h, run_addr[k], 1, stride, lens_addr[k], ob + k * batch, cb + 4 * k * batch)
+                  for k in range(nb)]
+            for k, t in enumerate(tk):
+                assert t and srv.wait(t) == 1
+                ok &= same(k, o[k], c[k])
+            if rep:
+                bursts.append(time.perf_counter() - t0)
+        burst_s = float(np.median(bursts))
+        peak = nb / burst_s
+        rows = []
+        for lv in levels:
+            lam = lv * peak
+            m = min(max_requests, max(30, int(lam)))
+            arrivals = np.cumsum(rng.exponential(1.0 / lam, m))
+            o, c, ob, cb = outputs(m)
+            tk = []
+            start = time.perf_counter()
+            for j, ta in enumerate(arrivals):
+                while time.perf_counter() - start < ta:
+                    pass
+                k = j % nb
+                tk.append(submit(srv.h, run_addr[k], 1, stride, lens_addr[k], ob + j * batch, cb + 4 * j * batch))
+            submit_s = time.perf_counter() - start
+            lat = []
+            for j, t in enumerate(tk):
+                assert t and srv.wait(t, release=False) == 1
+                a, b = srv.times_ns(t)
+                lat.append((b - a) * 1e-9)
+                ok &= same(j % nb, o[j], c[j])
+                srv.release(t)
+            rows.append({"offered_fraction_of_peak": lv, "offered_batches_per_s": lam, "batches": m,
+                         "achieved_submit_rate": m / max(1e-9, submit_s),
+                         "latency_ms": {"p50": _pct(lat, 50) * 1e3, "p99": _pct(lat, 99) * 1e3,
+                                        "p99.9": _pct(lat, 99.9) * 1e3}})
+        stats = srv.stats()
+    finally:
+        srv.close()
+    lib.verify_packets(*views[0])
+    t0 = time.perf_counter()
+    for k, (d, ln) in enumerate(views):
+        o, c = lib.verify_packets(d, ln)
+        ok &= same(k, o, c)
+    percall_s = time.perf_counter() - t0
+    return {"workload": f"{nb} batches of {batch} packets", "peak_packets_per_s": nb * batch / burst_s,
+            "burst_s": burst_s, "levels": rows,
+            "per_call_one_thread": {"packets_per_s": nb * batch / percall_s, "s": percall_s,
+                                    "latency_ms_per_batch": percall_s / nb * 1e3},
+            "results_identical": bool(ok), "server_stats": stats}
 
 
 def _pct(xs, q):

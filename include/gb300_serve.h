@@ -3,8 +3,8 @@
  * in the reference, which only has the synchronous one-batch calls).
  *
  * A server owns one GPU (the device current at creation) and a dispatcher
- * thread.  Requests -- an Ed25519 verify or sign job, or a PoH batch -- are
- * queued by any thread and admitted as launch slots and device memory free
+ * thread.  Requests -- an Ed25519 verify or sign job, a batch of Solana
+ * wire-format packets, or a PoH batch -- are queued by any thread and admitted as launch slots and device memory free
  * up (device memory held by in-flight requests stays below the configured
  * cap).  Signature requests that arrive while earlier ones are on the GPU
  * are merged into the next persistent launch (continuous batching) on
@@ -47,6 +47,19 @@ void gb300_server_destroy(gb300_server* s);
  * (> 0) or 0 when the job is invalid or alone exceeds the memory cap. */
 uint64_t gb300_server_submit_sigs(gb300_server* s, const gb300_sig_job* job);
 
+/* Queues a batch of Solana wire-format packets, as
+ * gb300_ed25519_verify_packets (gb300_packets.h) takes it: num_elems runs of
+ * elems[i].num packet slots `stride` bytes apart, packet_lens[total packets];
+ * on completion packet_out[i] = 1 iff packet i parsed and all its signatures
+ * verified, sig_counts[i] (nullable) = its signatures.  The descriptors in
+ * `elems` are copied; the packet data, lengths and outputs must stay valid
+ * until completion.  Batches of one stride merge into one launch that parses
+ * on the GPU.  Ticket, or 0 when the batch is invalid (no packets, null
+ * pointers, total slot bytes of 4 GiB or more) or alone exceeds the memory
+ * cap. */
+uint64_t gb300_server_submit_packets(gb300_server* s, const gpu_Elems* elems, uint32_t num_elems, uint32_t stride,
+                                     const uint32_t* packet_lens, uint8_t* packet_out, uint32_t* sig_counts);
+
 /* Queues a PoH batch (in place on hashes, as poh_verify_many); ticket or 0. */
 uint64_t gb300_server_submit_poh(gb300_server* s, uint8_t* hashes, const uint64_t* num_hashes, size_t num_elems);
 
@@ -65,11 +78,11 @@ void gb300_server_release(gb300_server* s, uint64_t ticket);
 int gb300_server_times(gb300_server* s, uint64_t ticket, int64_t* submit_ns, int64_t* done_ns);
 
 /* Timeline of the most recent launches as a JSON array of
- * [kind (0 signatures, 2 PoH), requests merged, items, admitted_ns,
- *  enqueued_ns, completed_ns, copy_in_ms, kernels_ms, copy_out_ms]: host
- * times of the launch, then the GPU time of its input copies, its kernels
- * and its result copy (CUDA events; -1 after a failure); returns the
- * length written. */
+ * [kind (0 signatures, 2 PoH, 3 wire packets), requests merged, items,
+ *  admitted_ns, enqueued_ns, completed_ns, copy_in_ms, kernels_ms,
+ *  copy_out_ms]: host times of the launch, then the GPU time of its input
+ * copies, its kernels and its result copy (CUDA events; -1 after a
+ * failure); returns the length written. */
 int gb300_server_trace(gb300_server* s, char* buf, size_t len);
 
 /* Counters as a JSON object; returns the length written. */

@@ -78,6 +78,9 @@ struct SigWork {
     // Set by launch_sig_batch: verify chunks of 8 signatures, four lanes each
     // (small batches); otherwise chunks of 32, one lane each.
     bool v_quad = false;
+    // Set by launch_sig_batch for count_dev launches: the kernel takes the
+    // four-lane form when *count_dev <= v_quad_max (0: never by count).
+    uint32_t v_quad_max = 0;
     // Caller's choice: -1 by batch size, kVerifySingle / kVerifyQuad to force.
     int v_form_hint = -1;
 };

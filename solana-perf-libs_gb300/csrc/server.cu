@@ -8,8 +8,11 @@
 //   * admission: while a signature slot is free, take queued verify/sign
 //     jobs in arrival order until the launch's item cap or the memory budget
 //     would be exceeded, and run them as ONE persistent launch (the mixed
-//     kernel of sig_batch.cu) on that slot's high-priority stream; likewise
-//     PoH batches on low-priority streams (persistent PoH kernel);
+//     kernel of sig_batch.cu) on that slot's high-priority stream.  Queued
+//     wire-format packet batches of one stride merge the same way into one
+//     parse + verify + reduce launch (packets.cu), whose signature count is
+//     known only on the device; a launch holds one of the two kinds.  PoH
+//     batches run on low-priority streams (persistent PoH kernel);
 //   * sleep on a condition variable when there is nothing to do (woken by
 //     submissions; polls the GPU every 20 us while work is in flight).
 // Slot buffers (device rings and page-locked staging) are sized at creation
@@ -52,11 +55,20 @@ bool page_locked(const void* p) {
 
 struct Req {
     uint64_t ticket = 0;
-    int kind = 0;                 // 0 verify, 1 sign, 2 poh
+    int kind = 0;                 // 0 verify, 1 sign, 2 poh, 3 wire packets
     gb300_sig_job job{};
     uint8_t* hashes = nullptr;
     const uint64_t* counts = nullptr;
-    uint64_t n = 0;               // items (signatures or entries)
+    // wire packets: the caller's runs of packet slots (descriptors copied at
+    // submission), data lengths and per-packet outputs
+    std::vector<gpu_Elems> elems;
+    uint32_t stride = 0;
+    const uint32_t* lens = nullptr;
+    uint8_t* pkt_out = nullptr;
+    uint32_t* sig_counts = nullptr;
+    uint64_t n = 0;               // items (signatures, entries or packets)
+    uint64_t ring_bytes = 0;      // packet bytes in the slot's ring
+    bool locked = false;          // packet bytes page-locked (checked at submission)
     uint64_t bytes = 0;           // device bytes while in flight
 };
 
@@ -68,7 +80,7 @@ struct Slot {
     // (kernels start), ev_out (results start copying), done (all copied)
     cudaEvent_t ev_in = nullptr, ev_run = nullptr, ev_out = nullptr;
     bool busy = false;
-    int kind = 0;                 // 0 signatures, 2 PoH
+    int kind = 0;                 // 0 signatures, 2 PoH, 3 wire packets
     DevBuf d_data, d_index, d_out, d_scratch;
     HostBuf h_stage, h_out;
     std::vector<Req> reqs;
@@ -119,6 +131,9 @@ uint64_t sig_bytes(const gb300_sig_job& j) {
     return j.packets_len + 16ull * j.num + (j.kind == 0 ? j.num : 64ull * j.num) + 64;
 }
 
+// Output layout of a packets launch: verdicts, then signature counts.
+uint64_t pkt_counts_off(uint64_t n) { return round_up(n, 256); }
+
 // Stage and launch the requests in S.reqs (signature jobs) on S.stream.
 cudaError_t launch_sigs(gb300_server* sv, Slot& S) {
     uint64_t nv = 0, ns = 0, total = 0;
@@ -126,7 +141,7 @@ cudaError_t launch_sigs(gb300_server* sv, Slot& S) {
     for (auto& r : S.reqs) {
         (r.kind == 0 ? nv : ns) += r.n;
         total += r.job.packets_len;
-        if (r.job.packets_len && locked) locked = page_locked(r.job.packets);
+        locked = locked && r.locked;
     }
     S.nv = nv;
     S.ns = ns;
@@ -195,6 +210,66 @@ cudaError_t launch_sigs(gb300_server* sv, Slot& S) {
     return cudaEventRecord(S.done, S.stream);
 }
 
+// Stage and launch the wire-packet requests in S.reqs (one stride) on
+// S.stream: packet slots into the ring (page-locked runs copied directly),
+// data lengths beside them, then the device parse / verify / reduce.
+cudaError_t launch_packets(gb300_server* sv, Slot& S) {
+    const uint64_t stride = S.reqs.front().stride;
+    uint64_t n = 0;
+    bool locked = true;
+    for (auto& r : S.reqs) {
+        n += r.n;
+        locked = locked && r.locked;
+    }
+    S.nv = n;
+    const uint64_t total = n * stride, lens_bytes = 4 * n, pk_off = round_up(lens_bytes, 256);
+    const uint64_t out_bytes = pkt_counts_off(n) + 4 * n;
+    const size_t ws_bytes = packets_workspace_size((uint32_t)n, stride);
+    cudaError_t e;
+    if ((e = S.d_data.ensure(total + 16, S.stream)) != cudaSuccess) return e;
+    if ((e = S.d_index.ensure(lens_bytes, S.stream)) != cudaSuccess) return e;
+    if ((e = S.d_out.ensure(out_bytes, S.stream)) != cudaSuccess) return e;
+    if ((e = S.d_scratch.ensure(ws_bytes, S.stream)) != cudaSuccess) return e;
+    if ((e = S.h_stage.ensure(pk_off + (locked ? 0 : total))) != cudaSuccess) return e;
+    if ((e = S.h_out.ensure(out_bytes)) != cudaSuccess) return e;
+    uint32_t* hl = static_cast<uint32_t*>(S.h_stage.p);
+    uint8_t* img = static_cast<uint8_t*>(S.h_stage.p) + pk_off;
+    uint8_t* dpk = static_cast<uint8_t*>(S.d_data.p);
+    uint64_t pos = 0;
+    if ((e = cudaEventRecord(S.ev_in, S.stream)) != cudaSuccess) return e;
+    for (auto& r : S.reqs) {
+        memcpy(hl + pos, r.lens, 4 * r.n);
+        uint64_t p = pos;
+        for (const gpu_Elems& g : r.elems) {
+            if (!g.num) continue;
+            const uint64_t b = (uint64_t)g.num * stride;
+            if (locked) {
+                e = cudaMemcpyAsync(dpk + p * stride, g.elems, b, cudaMemcpyHostToDevice, S.stream);
+                if (e != cudaSuccess) return e;
+            } else {
+                memcpy(img + p * stride, g.elems, b);
+            }
+            p += g.num;
+        }
+        pos += r.n;
+    }
+    if ((e = cudaMemcpyAsync(S.d_index.p, hl, lens_bytes, cudaMemcpyHostToDevice, S.stream)) != cudaSuccess)
+        return e;
+    if (!locked && (e = cudaMemcpyAsync(dpk, img, total, cudaMemcpyHostToDevice, S.stream)) != cudaSuccess)
+        return e;
+    uint8_t* dout = static_cast<uint8_t*>(S.d_out.p);
+    if ((e = cudaEventRecord(S.ev_run, S.stream)) != cudaSuccess) return e;
+    if ((e = launch_packets_verify(dpk, stride, (uint32_t)n, static_cast<const uint32_t*>(S.d_index.p),
+                                   S.d_scratch.p, S.d_scratch.cap, dout,
+                                   reinterpret_cast<uint32_t*>(dout + pkt_counts_off(n)), sv->info.tables,
+                                   sv->info.sig_threads, sv->info.sig_blocks_per_sm, sv->info.sms, S.stream,
+                                   sv->info.verify_window)) != cudaSuccess)
+        return e;
+    if ((e = cudaEventRecord(S.ev_out, S.stream)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(S.h_out.p, dout, out_bytes, cudaMemcpyDeviceToHost, S.stream)) != cudaSuccess) return e;
+    return cudaEventRecord(S.done, S.stream);
+}
+
 cudaError_t launch_pohs(gb300_server* sv, Slot& S) {
     uint64_t n = 0;
     for (auto& r : S.reqs) n += r.n;
@@ -238,6 +313,20 @@ void deliver(Slot& S) {
                 else memset(r.job.out, 0, 64ull * r.n);
                 os += r.n;
             }
+        }
+    } else if (S.kind == 3) {
+        const uint8_t* ho = static_cast<const uint8_t*>(S.h_out.p);
+        const uint32_t* hc = reinterpret_cast<const uint32_t*>(ho + pkt_counts_off(S.nv));
+        uint64_t pos = 0;
+        for (auto& r : S.reqs) {
+            if (S.err == cudaSuccess) {
+                memcpy(r.pkt_out, ho + pos, r.n);
+                if (r.sig_counts) memcpy(r.sig_counts, hc + pos, 4 * r.n);
+            } else {
+                memset(r.pkt_out, 0, r.n);
+                if (r.sig_counts) memset(r.sig_counts, 0, 4 * r.n);
+            }
+            pos += r.n;
         }
     } else if (S.err == cudaSuccess) {
         const uint8_t* st = static_cast<const uint8_t*>(S.h_stage.p);
@@ -305,30 +394,34 @@ void dispatcher(gb300_server* sv) {
         for (auto& S : sv->sig_slots) {
             if (S.busy || sv->pending_sig.empty()) continue;
             uint64_t items = 0, bytes = 0, pkt = 0;
+            const bool wire = sv->pending_sig.front().kind == 3;
+            const uint32_t stride = sv->pending_sig.front().stride;
             while (!sv->pending_sig.empty()) {
                 const Req& r = sv->pending_sig.front();
                 // merge while the launch fits the item cap, the memory budget
-                // and the slot's resident packet ring (no reallocation)
-                if (!S.reqs.empty() && (items + r.n > sv->max_items || sv->in_use + bytes + r.bytes > sv->cap ||
-                                        pkt + r.job.packets_len + 16 > S.d_data.cap))
+                // and the slot's resident packet ring (no reallocation); one
+                // launch holds wire packets of one stride or offset jobs
+                if (!S.reqs.empty() && ((r.kind == 3) != wire || (wire && r.stride != stride) ||
+                                        items + r.n > sv->max_items || sv->in_use + bytes + r.bytes > sv->cap ||
+                                        pkt + r.ring_bytes + 16 > S.d_data.cap))
                     break;
                 if (S.reqs.empty() && sv->in_use + r.bytes > sv->cap) break;   // wait for memory
                 items += r.n;
                 bytes += r.bytes;
-                pkt += r.job.packets_len;
+                pkt += r.ring_bytes;
                 S.reqs.push_back(r);
                 sv->pending_sig.pop_front();
             }
             if (S.reqs.empty()) continue;
             S.busy = true;
-            S.kind = 0;
+            S.kind = wire ? 3 : 0;
             S.bytes = bytes;
             sv->in_use += bytes;
             sv->launches_sig++;
             if (S.reqs.size() > sv->merged_max) sv->merged_max = S.reqs.size();
             S.t_admit = now_ns();
             lk.unlock();
-            S.err = launch_sigs(sv, S);
+            S.err = wire ? launch_packets(sv, S) : launch_sigs(sv, S);
             S.t_enqueued = now_ns();
             lk.lock();
             launched = true;
@@ -481,6 +574,8 @@ uint64_t gb300_server_submit_sigs(gb300_server* sv, const gb300_sig_job* job) {
     r.kind = (int)job->kind;
     r.job = *job;
     r.n = job->num;
+    r.ring_bytes = job->packets_len;
+    r.locked = !job->packets_len || page_locked(job->packets);
     r.bytes = sig_bytes(*job);
     if (r.bytes > sv->cap) return 0;   // a request above max_items runs in a launch of its own
     std::lock_guard<std::mutex> lk(sv->mu);
@@ -490,6 +585,38 @@ uint64_t gb300_server_submit_sigs(gb300_server* sv, const gb300_sig_job* job) {
     sv->pending_sig.push_back(r);
     sv->cv_work.notify_one();
     return r.ticket;
+}
+
+uint64_t gb300_server_submit_packets(gb300_server* sv, const gpu_Elems* elems, uint32_t num_elems, uint32_t stride,
+                                     const uint32_t* packet_lens, uint8_t* packet_out, uint32_t* sig_counts) {
+    if (!sv || !elems || num_elems == 0 || stride == 0 || !packet_lens || !packet_out) return 0;
+    Req r;
+    r.kind = 3;
+    r.stride = stride;
+    r.lens = packet_lens;
+    r.pkt_out = packet_out;
+    r.sig_counts = sig_counts;
+    for (uint32_t i = 0; i < num_elems; i++) {
+        if (elems[i].num && !elems[i].elems) return 0;
+        r.n += elems[i].num;
+    }
+    // packet offsets are 32-bit, as in the one-call form
+    if (r.n == 0 || r.n * stride > 0xffffffffull) return 0;
+    r.elems.assign(elems, elems + num_elems);
+    r.locked = true;
+    for (const gpu_Elems& g : r.elems)
+        if (g.num && r.locked) r.locked = page_locked(g.elems);
+    r.ring_bytes = r.n * stride;
+    r.bytes = r.ring_bytes + 4 * r.n + pkt_counts_off(r.n) + 4 * r.n +
+              packets_workspace_size((uint32_t)r.n, stride) + 64;
+    if (r.bytes > sv->cap) return 0;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    const uint64_t t = r.ticket = sv->next_ticket++;
+    sv->status[t] = 0;
+    sv->times[t] = {now_ns(), -1};
+    sv->pending_sig.push_back(std::move(r));
+    sv->cv_work.notify_one();
+    return t;
 }
 
 uint64_t gb300_server_submit_poh(gb300_server* sv, uint8_t* hashes, const uint64_t* num_hashes, size_t num_elems) {

@@ -27,8 +27,8 @@ namespace {
 
 // Chunk counts of a launch: verify chunks (32 signatures, or 8 in quad
 // mode), then sign chunks of 32.
-__host__ __device__ __forceinline__ uint32_t verify_chunks(const SigWork& w, uint32_t vn) {
-    if (w.v_quad) return (vn + 7u) / 8u;
+__host__ __device__ __forceinline__ uint32_t verify_chunks(const SigWork& w, uint32_t vn, bool quad) {
+    if (quad) return (vn + 7u) / 8u;
     return w.count_dev ? (vn + 31u) / 32u : w.sign_base / 32u;
 }
 __host__ __device__ __forceinline__ uint32_t sign_chunks(const SigWork& w) {
@@ -55,7 +55,8 @@ __global__ void __launch_bounds__(T, MINB) sig_persistent_kernel(SigWork w) {
     __syncthreads();
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t vn = w.count_dev ? *w.count_dev : w.v.n;
-    const uint32_t vchunks = verify_chunks(w, vn);
+    const bool quad = w.v_quad || (w.v_quad_max && vn <= w.v_quad_max);   // launch-uniform
+    const uint32_t vchunks = verify_chunks(w, vn, quad);
     const uint32_t chunks = vchunks + sign_chunks(w);
     for (;;) {
         uint32_t c = 0;
@@ -63,7 +64,7 @@ __global__ void __launch_bounds__(T, MINB) sig_persistent_kernel(SigWork w) {
         c = __shfl_sync(0xffffffffu, c, 0);
         if (c >= chunks) break;
         if (c < vchunks) {
-            if (w.v_quad) {
+            if (quad) {
                 // every lane runs an item (past the end: the last one again,
                 // result dropped) so the whole warp meets every shuffle
                 const uint32_t i = c * 8u + (lane >> 2);
@@ -102,7 +103,9 @@ cudaError_t launch_t(const SigWork& w, int blocks_per_sm, int sms, cudaStream_t 
     if (e != cudaSuccess) return e;
     if (maxb < 1) maxb = 1;
     int b = blocks_per_sm < 1 ? maxb : (blocks_per_sm < maxb ? blocks_per_sm : maxb);
-    uint32_t warps_needed = verify_chunks(w, w.v.n) + sign_chunks(w);
+    // (a launch that may take the four-lane form by its device count is
+    // sized for it)
+    uint32_t warps_needed = verify_chunks(w, w.v.n, w.v_quad || w.v_quad_max > 0) + sign_chunks(w);
     uint32_t grid = (uint32_t)(b * sms);
     uint32_t per_block = T / 32;
     if (grid * per_block > warps_needed) grid = (warps_needed + per_block - 1) / per_block;
@@ -127,9 +130,16 @@ cudaError_t launch_sig_batch(const SigWork& w_in, int threads, int blocks_per_sm
     if (e != cudaSuccess) return e;
     const bool w5 = w.v.window == 5;
     // a launch with chunks for 3 blocks of 128 threads on every SM runs the
-    // build capped at 3 blocks per SM (1 minimum otherwise)
-    const uint64_t warps = (uint64_t)verify_chunks(w, w.v.n) + sign_chunks(w);
-    const bool full = threads != 64 && threads != 256 && !w5 && blocks_per_sm < 1 && warps >= 12ull * (uint64_t)sms;
+    // build capped at 3 blocks per SM (1 minimum otherwise).  Not a count_dev
+    // launch: its size is a capacity, ~10x the signatures of a packet batch
+    // (16,384 packets: 2.34 ms in the capped build against 1.66 ms).
+    const uint64_t warps = (uint64_t)verify_chunks(w, w.v.n, w.v_quad) + sign_chunks(w);
+    const bool full = threads != 64 && threads != 256 && !w5 && blocks_per_sm < 1 && !w.count_dev &&
+                      warps >= 12ull * (uint64_t)sms;
+    // a count_dev launch sized above the four-lane limit still takes the
+    // four-lane form when its device count turns out small
+    w.v_quad_max = 0;
+    if (w.count_dev && !w.v_quad && form != kVerifySingle) w.v_quad_max = (uint32_t)(64u * (uint32_t)sms);
     switch (threads) {
         case 64: return w5 ? launch_t<64, 5, 1>(w, blocks_per_sm, sms, s) : launch_t<64, 4, 1>(w, blocks_per_sm, sms, s);
         case 256:

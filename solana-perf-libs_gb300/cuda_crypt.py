@@ -408,6 +408,9 @@ class Server:
         L.gb300_server_stats.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]
         L.gb300_server_times.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(ctypes.c_int64),
                                          ctypes.POINTER(ctypes.c_int64)]
+        L.gb300_server_submit_packets.argtypes = [ctypes.c_void_p, ctypes.POINTER(GpuElems), ctypes.c_uint32,
+                                                  ctypes.c_uint32, _u32p, _u8p, _u32p]
+        L.gb300_server_submit_packets.restype = ctypes.c_uint64
         cfg = ServerConfig(device_memory_cap, sig_slots, poh_slots, max_items_per_launch)
         self.h = L.gb300_server_create(ctypes.byref(cfg))
         if not self.h:
@@ -428,6 +431,30 @@ class Server:
         if t:
             self._keep[t] = (pk, arrs, out, j)
         return t, out
+
+    def submit_packets(self, data: np.ndarray, lens, batches: int = 1, counts: bool = True):
+        """Queues wire-format packets: `data` (n, stride) uint8 slots split
+        into `batches` gpu_Elems runs.  Returns (ticket, packet verdicts,
+        signatures per packet or None), filled when the ticket completes."""
+        assert data.dtype == np.uint8 and data.ndim == 2 and data.flags["C_CONTIGUOUS"]
+        n, stride = data.shape
+        lens = np.ascontiguousarray(lens, dtype=np.uint32)
+        elems = (GpuElems * batches)()
+        if batches == 1:
+            elems[0].elems = _p(data, _u8p)
+            elems[0].num = n
+        else:
+            cuts = np.linspace(0, n, batches + 1).astype(int)
+            for i in range(batches):
+                elems[i].elems = _p(data[cuts[i]:], _u8p) if cuts[i] < n else None
+                elems[i].num = int(cuts[i + 1] - cuts[i])
+        out = np.zeros(n, dtype=np.uint8)
+        cnt = np.zeros(n, dtype=np.uint32) if counts else None
+        t = self.L.gb300_server_submit_packets(self.h, elems, batches, stride, _p(lens, _u32p), _p(out, _u8p),
+                                               _p(cnt, _u32p) if counts else None)
+        if t:
+            self._keep[t] = (data, lens, out, cnt)
+        return t, out, cnt
 
     def submit_poh(self, hashes: np.ndarray, num_hashes):
         nh = np.ascontiguousarray(num_hashes, dtype=np.uint64)

@@ -267,10 +267,11 @@ def _message(rng, signer_pks, versioned: bool) -> bytes:
 
 
 def wire_packets(keypairs, sign, n: int = 4096, corrupt_frac: float = 0.05, malformed_frac: float = 0.03,
-                 seed: int = 11, stride: int = WIRE_STRIDE) -> WirePackets:
-    """`n` packets; signatures made with `keypairs` / `sign` as elsewhere."""
+                 seed: int = 11, stride: int = WIRE_STRIDE, signers=(1, 1, 1, 2, 2, 3, 4)) -> WirePackets:
+    """`n` packets with signer counts drawn from `signers`; signatures made
+    with `keypairs` / `sign` as elsewhere."""
     rng = np.random.default_rng(seed)
-    nsig = rng.choice([1, 1, 1, 2, 2, 3, 4], n)
+    nsig = rng.choice(list(signers), n)
     total = int(nsig.sum())
     pk, sk = keypairs(rng.integers(0, 256, (total, 32), dtype=np.uint8))
     msgs, first = [], 0

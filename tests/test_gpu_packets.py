@@ -102,3 +102,15 @@ def test_verify_packets_edges(lib, oracle):
     exp, _, counts = oracle.verify_wire_packets(big.data, big.stride, big.lens, nthreads())
     out, got = lib.verify_packets(big.data, big.lens, batches=4)
     assert np.array_equal(out, exp) and np.array_equal(got, counts)
+
+
+@pytest.mark.parametrize("n", [2000, 2800])
+def test_verify_packets_form_by_device_count(lib, oracle, n):
+    """Four signers per packet: 8,000 and 11,200 signatures in launches sized
+    by capacity (20 per packet) for either verify form, so the kernel picks
+    the form from the parsed count (four lanes up to 64 per SM, else one)."""
+    w = _wire(oracle, n, 39 + n, corrupt_frac=0.05, malformed_frac=0.02, signers=(4,))
+    exp, _, counts = oracle.verify_wire_packets(w.data, w.stride, w.lens, nthreads())
+    assert counts.max() == 4
+    out, got = lib.verify_packets(w.data, w.lens)
+    assert np.array_equal(out, exp) and np.array_equal(got, counts)
