@@ -11,7 +11,8 @@
  *
  * All computation runs on the GPU; functions return after their results are
  * in the caller's buffers.  Thread-safe: calls are spread round-robin over
- * up to 8 GPUs x 8 queues, each queue serialised by its own lock.
+ * up to 8 GPUs, then to the first idle of 8 queues on that GPU, each queue
+ * serialised by its own lock.
  */
 #ifndef GB300_CRYPT_ED25519_H
 #define GB300_CRYPT_ED25519_H

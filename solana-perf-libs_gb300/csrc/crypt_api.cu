@@ -4,8 +4,11 @@
 // Replaces the reference's host drivers and context pool
 // (src/cuda-ecc-ed25519/gpu_ctx.cu:8-165, verify.cu:240-340,
 // sign.cu:76-145, src/cuda-poh-verify/poh_verify.cu:29-144).
-// Same pool shape (up to 8 GPUs x 8 queues, round-robin, one lock per
-// queue, grow-only device buffers) shared by every entry point, plus:
+// Same pool shape (up to 8 GPUs x 8 queues, one lock per queue, grow-only
+// device buffers) shared by every entry point; calls go round-robin over
+// the GPUs as in the reference, but within a GPU to its first idle queue
+// rather than the next one, so that a lone caller keeps reusing one queue's
+// buffers and captured graphs.  In addition:
 //   * a grow-only page-locked staging buffer per queue: the four per-
 //     signature index arrays and the packets go to the GPU in one copy
 //     (packets that the caller page-locked with cuda_host_register are
@@ -31,6 +34,7 @@
 #include "kernels.h"
 #include "tables.cuh"
 #include "host_buffers.h"
+#include "host_copy.h"
 
 #include <functional>
 
@@ -162,17 +166,28 @@ struct Lease {
     }
 };
 
-// Round-robin (gpu, queue) pick, then the queue's lock (reference
-// gpu_ctx.cu:46-73).
+// GPU round-robin, then the GPU's first idle queue (the next one in turn
+// when all are busy), then the queue's lock (reference gpu_ctx.cu:46-73
+// picks the next queue in turn every time: a caller issuing one call after
+// another then meets every queue's first-use buffer growth and graph
+// capture; measured on GB300 for 131 MB ragged batches: 15.4 ms per call
+// in turn against 9.2 ms on the warm queue).
 bool acquire(Lease& L) {
     std::unique_lock<std::mutex> lk(g_mu);
     if (!init_locked()) return false;
     Device& D = g_dev[g_next_gpu % (uint32_t)g_num_gpus];
     g_next_gpu++;
-    Queue& Q = D.q[D.next_queue % kQueues];
-    D.next_queue++;
+    Queue* pick = nullptr;
+    for (int k = 0; k < kQueues && !pick; k++)
+        if (D.q[k].mu.try_lock()) pick = &D.q[k];        // non-blocking under g_mu
+    const bool held = pick != nullptr;
+    if (!held) {
+        pick = &D.q[D.next_queue % kQueues];
+        D.next_queue++;
+    }
     lk.unlock();
-    Q.mu.lock();
+    Queue& Q = *pick;
+    if (!held) Q.mu.lock();
     L.dev = &D;
     L.q = &Q;
     cudaSetDevice(D.id);
@@ -464,12 +479,14 @@ cudaError_t run_sig_batch(Lease& L, cudaStream_t s, bool sign, const gpu_Elems* 
         }
     } else {
         uint8_t* img = static_cast<uint8_t*>(Q.h_stage.p) + stage_pk_off;
+        std::vector<gb300::CopyPiece> pcs;
         uint64_t cur = 0;
         for (uint32_t i = 0; i < num_elems; i++) {
             uint64_t b = (uint64_t)elems[i].num * message_size;
-            if (b) memcpy(img + cur, elems[i].elems, b);
+            if (b) pcs.push_back({img + cur, elems[i].elems, b});
             cur += b;
         }
+        gb300::CopyPool::copy(pcs.data(), pcs.size());
         if (total_bytes) TRY(cudaMemcpyAsync(dpk, img, total_bytes, cudaMemcpyHostToDevice, s));
     }
 
@@ -978,6 +995,7 @@ int gb300_ed25519_batch(const gb300_sig_job* jobs, uint32_t num_jobs) {
         uint8_t* img = static_cast<uint8_t*>(Q.h_stage.p) + pk_off;
         uint8_t* dpk = static_cast<uint8_t*>(Q.d_data.p);
         uint64_t base = 0, iv = 0, is = 0;
+        std::vector<gb300::CopyPiece> pcs;
         for (uint32_t j = 0; j < num_jobs; j++) {
             const gb300_sig_job& J = jobs[j];
             if (J.num == 0) continue;
@@ -998,11 +1016,12 @@ int gb300_ed25519_batch(const gb300_sig_job* jobs, uint32_t num_jobs) {
                 if (all_locked)
                     TRY(cudaMemcpyAsync(dpk + base, J.packets, J.packets_len, cudaMemcpyHostToDevice, s));
                 else
-                    memcpy(img + base, J.packets, J.packets_len);
+                    pcs.push_back({img + base, J.packets, J.packets_len});
             }
             pos += J.num;
             base += J.packets_len;
         }
+        gb300::CopyPool::copy(pcs.data(), pcs.size());
         TRY(cudaMemcpyAsync(Q.d_index.p, Q.h_stage.p, idx_bytes, cudaMemcpyHostToDevice, s));
         if (!all_locked && total) TRY(cudaMemcpyAsync(dpk, img, total, cudaMemcpyHostToDevice, s));
         const uint32_t* dv = static_cast<const uint32_t*>(Q.d_index.p);
@@ -1127,13 +1146,15 @@ int gb300_ed25519_verify_packets(const gpu_Elems* elems, uint32_t num_elems, uin
         TRY(cudaMemcpyAsync(dlens, Q.h_stage.p, lens_bytes, cudaMemcpyHostToDevice, s));
         uint64_t cur = 0;
         uint8_t* img = static_cast<uint8_t*>(Q.h_stage.p) + pk_off;
+        std::vector<gb300::CopyPiece> pcs;
         for (uint32_t i = 0; i < num_elems; i++) {
             const uint64_t b = (uint64_t)elems[i].num * stride;
             if (!b) continue;
             if (all_locked) TRY(cudaMemcpyAsync(dpk + cur, elems[i].elems, b, cudaMemcpyHostToDevice, s));
-            else memcpy(img + cur, elems[i].elems, b);
+            else pcs.push_back({img + cur, elems[i].elems, b});
             cur += b;
         }
+        gb300::CopyPool::copy(pcs.data(), pcs.size());
         if (!all_locked) TRY(cudaMemcpyAsync(dpk, img, total, cudaMemcpyHostToDevice, s));
         uint8_t* dout = static_cast<uint8_t*>(Q.d_out.p);
         uint32_t* dcnt = reinterpret_cast<uint32_t*>(dout + out_off);

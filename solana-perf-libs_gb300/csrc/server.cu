@@ -35,6 +35,7 @@
 #include "ed25519.h"
 #include "gb300_serve.h"
 #include "host_buffers.h"
+#include "host_copy.h"
 #include "kernels.h"
 #include "tables.cuh"
 
@@ -160,6 +161,7 @@ cudaError_t launch_sigs(gb300_server* sv, Slot& S) {
     uint8_t* img = static_cast<uint8_t*>(S.h_stage.p) + pk_off;
     uint8_t* dpk = static_cast<uint8_t*>(S.d_data.p);
     uint64_t base = 0, iv = 0, is = 0;
+    std::vector<gb300::CopyPiece> pcs;
     if ((e = cudaEventRecord(S.ev_in, S.stream)) != cudaSuccess) return e;
     for (auto& r : S.reqs) {
         const gb300_sig_job& J = r.job;
@@ -180,12 +182,13 @@ cudaError_t launch_sigs(gb300_server* sv, Slot& S) {
                 e = cudaMemcpyAsync(dpk + base, J.packets, J.packets_len, cudaMemcpyHostToDevice, S.stream);
                 if (e != cudaSuccess) return e;
             } else {
-                memcpy(img + base, J.packets, J.packets_len);
+                pcs.push_back({img + base, J.packets, J.packets_len});
             }
         }
         pos += J.num;
         base += J.packets_len;
     }
+    gb300::CopyPool::copy(pcs.data(), pcs.size());
     if ((e = cudaMemcpyAsync(S.d_index.p, S.h_stage.p, idx_bytes, cudaMemcpyHostToDevice, S.stream)) != cudaSuccess)
         return e;
     if (!locked && total && (e = cudaMemcpyAsync(dpk, img, total, cudaMemcpyHostToDevice, S.stream)) != cudaSuccess)
@@ -236,6 +239,7 @@ cudaError_t launch_packets(gb300_server* sv, Slot& S) {
     uint8_t* img = static_cast<uint8_t*>(S.h_stage.p) + pk_off;
     uint8_t* dpk = static_cast<uint8_t*>(S.d_data.p);
     uint64_t pos = 0;
+    std::vector<gb300::CopyPiece> pcs;
     if ((e = cudaEventRecord(S.ev_in, S.stream)) != cudaSuccess) return e;
     for (auto& r : S.reqs) {
         memcpy(hl + pos, r.lens, 4 * r.n);
@@ -247,12 +251,13 @@ cudaError_t launch_packets(gb300_server* sv, Slot& S) {
                 e = cudaMemcpyAsync(dpk + p * stride, g.elems, b, cudaMemcpyHostToDevice, S.stream);
                 if (e != cudaSuccess) return e;
             } else {
-                memcpy(img + p * stride, g.elems, b);
+                pcs.push_back({img + p * stride, g.elems, b});
             }
             p += g.num;
         }
         pos += r.n;
     }
+    gb300::CopyPool::copy(pcs.data(), pcs.size());
     if ((e = cudaMemcpyAsync(S.d_index.p, hl, lens_bytes, cudaMemcpyHostToDevice, S.stream)) != cudaSuccess)
         return e;
     if (!locked && (e = cudaMemcpyAsync(dpk, img, total, cudaMemcpyHostToDevice, S.stream)) != cudaSuccess)

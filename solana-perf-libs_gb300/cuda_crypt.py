@@ -230,6 +230,20 @@ class CudaCrypt:
     def ed25519_batch(self, jobs) -> list:
         """jobs: list of (SigPackets, kind).  Returns one output array per job
         (verdicts for kind 0, (n, 64) signatures for kind 1)."""
+        return self.ed25519_batch_run(self.ed25519_batch_prepare(jobs))
+
+    def ed25519_batch_run(self, prepared) -> list:
+        """gb300_ed25519_batch on arguments from ed25519_batch_prepare (the
+        call alone, as a compiled caller makes it); returns the outputs."""
+        arr, n, _, outs = prepared
+        rc = self.lib.gb300_ed25519_batch(arr, n)
+        if rc != 0:
+            raise RuntimeError(f"gb300_ed25519_batch: cudaError {rc}")
+        return outs
+
+    def ed25519_batch_prepare(self, jobs):
+        """The gb300_sig_job array for `jobs`, the arrays it points to and
+        the output arrays it fills."""
         keep, outs = [], []
         arr = (SigJob * max(1, len(jobs)))()
         for k, (sp, kind) in enumerate(jobs):
@@ -246,10 +260,7 @@ class CudaCrypt:
             j.message_lens, j.public_key_offsets, j.key_offsets, j.message_start_offsets = \
                 [_p(a, _u32p) for a in arrs]
             j.num, j.kind, j.out = n, kind, _p(out, _u8p)
-        rc = self.lib.gb300_ed25519_batch(arr, len(jobs))
-        if rc != 0:
-            raise RuntimeError(f"gb300_ed25519_batch: cudaError {rc}")
-        return outs
+        return arr, len(jobs), keep, outs
 
     def poh_verify_batch(self, hashes: np.ndarray, num_hashes) -> int:
         """In place on `hashes` (uint8, n*32), like poh_verify_many."""
