@@ -28,7 +28,9 @@ int gb300_int_peak_launch(int kind, uint32_t blocks, uint32_t threads, uint32_t 
  *   1  one warp per 32 chains, four warps per block
  *   2  a schedule warp and a round warp per 32 chains, one pair per block
  *   3  two such pairs per block
- *   4  no queue: one pair per 32 consecutive entries (`warps` unused).
+ *   4  no queue: one pair per 32 consecutive entries (`warps` unused)
+ *   5  form 2 with `warps`, or form 0 with 16 x SM count warps, chosen on the
+ *      device from the longest count and the sum of the counts.
  * Same results as every other PoH entry point; used to test and time each
  * form.  Returns a cudaError_t. */
 int gb300_poh_verify_batch_shape(uint8_t* hashes, const uint64_t* num_hashes, uint64_t num_elems, void* workspace,

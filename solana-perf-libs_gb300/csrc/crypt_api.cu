@@ -849,15 +849,18 @@ int gb300_poh_verify_batch_device(uint8_t* hashes, const uint64_t* num_hashes, u
     Device* D = current_device();
     if (!D) return (int)cudaErrorNoDevice;
     const Tuning& T = tuning_for(*D);
+    // the counts are in device memory: a paired tuning lets the device
+    // choose between paired and single warps from them (kPohAuto), as
+    // poh_host_batch_shape does from host counts
     return (int)launch_poh_batch(hashes, num_hashes, num_elems, workspace, 4 * D->sms * T.poh_warps_per_smsp,
-                                 static_cast<cudaStream_t>(stream), T.poh_form);
+                                 static_cast<cudaStream_t>(stream), T.poh_form == kPohPair ? kPohAuto : T.poh_form);
 }
 
 int gb300_poh_verify_batch_shape(uint8_t* hashes, const uint64_t* num_hashes, uint64_t num_elems, void* workspace,
                                  size_t workspace_bytes, int warps, int form, void* stream) {
     if (num_elems == 0) return 0;
     if (int rc = poh_batch_device_checks(hashes, num_hashes, num_elems, workspace, workspace_bytes)) return rc;
-    if (form < kPohSingle || form > kPohPairDirect) return (int)cudaErrorInvalidValue;
+    if (form < kPohSingle || form > kPohAuto) return (int)cudaErrorInvalidValue;
     Device* D = current_device();
     if (!D) return (int)cudaErrorNoDevice;
     if (warps < 1 || warps > 64 * D->sms) return (int)cudaErrorInvalidValue;

@@ -54,6 +54,7 @@ enum PohBatchForm : int {
     kPohPair = 2,           // schedule warp + round warp per 32 chains, one pair per block
     kPohPackedPair = 3,     // two such pairs per block (fewer SMs)
     kPohPairDirect = 4,     // no queue: one pair per 32 consecutive entries (workspace unused)
+    kPohAuto = 5,           // kPohPair or kPohSingle (16 x SMs warps), chosen on the device from the counts
 };
 size_t poh_batch_workspace_size(uint64_t n);
 cudaError_t launch_poh_batch(uint8_t* hashes, const uint64_t* counts, uint64_t n, void* workspace, int warps,

@@ -31,17 +31,48 @@ struct PohBatchScratch {
     uint32_t hist[kBuckets];
     uint32_t cursor[kBuckets];
     uint32_t next;              // queue head
-    uint32_t pad[3];
+    uint32_t choice;            // kPohAuto: 0 undecided, kChosePair or kChoseSingle
+    uint64_t total, longest;    // kPohAuto: sum and maximum of the counts
     uint32_t order[1];          // n entries
 };
+constexpr uint32_t kChosePair = 1, kChoseSingle = 2;
 
 __device__ __forceinline__ uint32_t bswap_u32(uint32_t x) { return __byte_perm(x, 0, 0x0123); }
 
 __device__ __forceinline__ int bucket_of(uint64_t c) { return c ? 64 - __clzll((long long)c) : 0; }
 
-__global__ void poh_hist_kernel(const uint64_t* counts, uint64_t n, PohBatchScratch* s) {
+// Bucket counts; with `totals`, also the sum and maximum of the counts
+// (warp-reduced, one atomic per warp).
+__global__ void poh_hist_kernel(const uint64_t* counts, uint64_t n, PohBatchScratch* s, bool totals) {
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) atomicAdd(&s->hist[bucket_of(counts[i])], 1u);
+    const uint64_t c = i < n ? counts[i] : 0;
+    if (i < n) atomicAdd(&s->hist[bucket_of(c)], 1u);
+    if (!totals) return;
+    uint64_t sum = c, mx = c;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sum += __shfl_down_sync(0xffffffffu, sum, o);
+        const uint64_t m = __shfl_down_sync(0xffffffffu, mx, o);
+        mx = m > mx ? m : mx;
+    }
+    if ((threadIdx.x & 31u) == 0) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(&s->total), (unsigned long long)sum);
+        atomicMax(reinterpret_cast<unsigned long long*>(&s->longest), (unsigned long long)mx);
+    }
+}
+
+// kPohAuto: paired warps run a chain fastest (~1,900 cycles per hash on
+// GB300) but hold two warps per 32 chains; single warps, four per
+// sub-partition, take ~2,550 cycles per hash alone and share the ALU pipe at
+// ~77.5 cycles per hash per sub-partition.  The shape with the smaller
+// makespan estimate runs (single warps only when 10 % shorter), as the host
+// forms decide from host counts.
+__global__ void poh_choose_kernel(PohBatchScratch* s, uint32_t sms) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const double L = (double)s->longest, T = (double)s->total;
+    const double pair = fmax(L * 1900.0, T * 1900.0 / (64.0 * sms));
+    const double single = fmax(L * 2550.0, T * 77.5 / (4.0 * sms));
+    s->choice = single < 0.9 * pair ? kChoseSingle : kChosePair;
 }
 
 // single warp: cursor[b] = number of entries in buckets above b (longest first)
@@ -100,6 +131,7 @@ static __device__ __noinline__ HashWords single_run(HashWords in, uint64_t r, ui
 template <int BW>
 __global__ void __launch_bounds__(32 * BW) poh_persistent_kernel(uint8_t* hashes, const uint64_t* counts, uint32_t n,
                                                                  PohBatchScratch* s, uint32_t one) {
+    if (s && s->choice == kChosePair) return;            // kPohAuto picked the other shape
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     uint64_t rem = 0;
@@ -342,6 +374,7 @@ template <int P>
 __global__ void __launch_bounds__(64 * P) poh_pair_persistent_kernel(uint8_t* hashes, const uint64_t* counts,
                                                                      uint32_t n, PohBatchScratch* s, uint32_t one) {
     static_assert(P >= 1 && P <= kMaxPairsPerBlock, "pairs per block");
+    if (s && s->choice == kChoseSingle) return;          // kPohAuto picked the other shape
     __shared__ uint64_t run_len[P];
     const uint32_t warp = threadIdx.x >> 5, pair = warp >> 1, role = warp & 1u;
     const uint32_t first = (blockIdx.x * P + pair) * 32u;   // direct mode only
@@ -370,10 +403,26 @@ cudaError_t launch_poh_batch(uint8_t* hashes, const uint64_t* counts, uint64_t n
     cudaError_t e = cudaMemsetAsync(sc, 0, sizeof(PohBatchScratch), s);
     if (e != cudaSuccess) return e;
     const unsigned blocks = (unsigned)((n + 255) / 256);
-    poh_hist_kernel<<<blocks, 256, 0, s>>>(counts, n, sc);
+    poh_hist_kernel<<<blocks, 256, 0, s>>>(counts, n, sc, form == kPohAuto);
     poh_scan_kernel<<<1, 32, 0, s>>>(sc);
     poh_scatter_kernel<<<blocks, 256, 0, s>>>(counts, n, sc);
     const uint64_t need = (n + 31) / 32;               // 32-lane groups
+    if (form == kPohAuto) {
+        // both shapes are enqueued; the one not chosen exits at its first
+        // instruction.  Paired: `warps` as given; single: four warps per
+        // sub-partition, one per block.
+        int dev = 0, sms = 0;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+        poh_choose_kernel<<<1, 32, 0, s>>>(sc, (uint32_t)sms);
+        const uint64_t pmax = warps / 2 > 0 ? (uint64_t)(warps / 2) : 1;
+        const uint64_t pairs = need < pmax ? need : pmax;
+        poh_pair_persistent_kernel<1><<<(unsigned)pairs, 64, 0, s>>>(hashes, counts, (uint32_t)n, sc, 1u);
+        const uint64_t smax = 16ull * (uint64_t)sms;
+        const uint64_t singles = need < smax ? need : smax;
+        poh_persistent_kernel<1><<<(unsigned)singles, 32, 0, s>>>(hashes, counts, (uint32_t)n, sc, 1u);
+        return cudaGetLastError();
+    }
     const uint64_t wmax = (uint64_t)(warps > 0 ? warps : 1);
     const uint64_t nwarps = need < wmax ? need : wmax;  // single forms: one warp per group
     const uint64_t pmax = wmax / 2 > 0 ? wmax / 2 : 1;  // paired forms: `warps` counts both warps of a pair
@@ -458,10 +507,11 @@ extern "C" int gb300_poh_verify_batch_static(uint8_t* hashes, const uint64_t* nu
         sms = g_static_sms[dev];
     }
     // The array keeps the previous call's contents; launch_poh_batch clears
-    // the header (bucket counts, cursors, queue head) on every call and
-    // rewrites the entry order in full.  Paired warps, one warp per SM
-    // sub-partition: the fastest form measured on GB300 (this entry point
-    // runs no autotuning, which would allocate).
+    // the header (bucket counts, cursors, queue head, shape choice) on every
+    // call and rewrites the entry order in full.  Paired warps, one warp per
+    // SM sub-partition, unless the counts make single warps faster (chosen
+    // on the device; this entry point runs no autotuning, which would
+    // allocate).
     return (int)launch_poh_batch(hashes, num_hashes, num_elems, scratch, 4 * sms, static_cast<cudaStream_t>(stream),
-                                 kPohPair);
+                                 kPohAuto);
 }

@@ -278,11 +278,11 @@ class CudaCrypt:
         if rc != 0:
             raise RuntimeError(f"gb300_poh_verify_batch_device: cudaError {rc}")
 
-    POH_SINGLE, POH_PACKED_SINGLE, POH_PAIR, POH_PACKED_PAIR, POH_PAIR_DIRECT = 0, 1, 2, 3, 4
+    POH_SINGLE, POH_PACKED_SINGLE, POH_PAIR, POH_PACKED_PAIR, POH_PAIR_DIRECT, POH_AUTO = 0, 1, 2, 3, 4, 5
 
     def poh_verify_batch_shape(self, hashes, num_hashes, workspace, warps, form, stream=0) -> None:
         """Device PoH batch with a forced persistent launch shape (diagnostic);
-        form: POH_SINGLE, POH_PACKED_SINGLE, POH_PAIR, POH_PACKED_PAIR or POH_PAIR_DIRECT."""
+        form: POH_SINGLE, POH_PACKED_SINGLE, POH_PAIR, POH_PACKED_PAIR, POH_PAIR_DIRECT or POH_AUTO."""
         rc = self.lib.gb300_poh_verify_batch_shape(hashes.data_ptr(), num_hashes.data_ptr(), num_hashes.numel(),
                                                    workspace.data_ptr(), workspace.numel() * workspace.element_size(),
                                                    warps, form, stream)

@@ -129,7 +129,7 @@ def test_tuning_report(lib):
 
 
 @pytest.mark.parametrize("form,warps_per_sm", [(0, 4), (0, 8), (0, 1), (1, 4), (2, 4), (2, 8), (2, 2),
-                                               (3, 4), (3, 2), (4, 4)])
+                                               (3, 4), (3, 2), (4, 4), (5, 4)])
 def test_poh_batch_every_launch_shape(lib, oracle, form, warps_per_sm):
     """Single, packed, paired and packed-paired persistent forms, at several
     residencies (odd pair counts included), give the oracle's chains (ragged
@@ -148,7 +148,7 @@ def test_poh_batch_every_launch_shape(lib, oracle, form, warps_per_sm):
     assert np.array_equal(dh.cpu().numpy(), exp)
 
 
-@pytest.mark.parametrize("form", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("form", [0, 1, 2, 3, 4, 5])
 def test_poh_batch_forms_few_chains(lib, oracle, form):
     """Fewer chains than one warp (a partly empty pair and block)."""
     torch = pytest.importorskip("torch")
@@ -167,9 +167,36 @@ def test_poh_batch_shape_rejects_bad_shapes(lib):
     dh = torch.zeros((4, 32), dtype=torch.uint8, device="cuda")
     dc = torch.ones(4, dtype=torch.int64, device="cuda")
     ws = torch.empty(lib.poh_batch_workspace_size(4), dtype=torch.uint8, device="cuda")
-    for warps, form in ((0, 0), (64, 5), (64, -1), (10 ** 6, 0)):
+    for warps, form in ((0, 0), (64, 6), (64, -1), (10 ** 6, 0)):
         with pytest.raises(RuntimeError):
             lib.poh_verify_batch_shape(dh, dc, ws, warps, form)
+
+
+@pytest.mark.parametrize("uniform", [True, False])
+def test_poh_batch_device_chooses_shape(lib, oracle, uniform):
+    """The device form picks paired or single warps from the counts on the
+    device: uniform counts over many chains (single warps: the total bounds
+    the makespan) and ragged ones (paired: the longest chain does); both
+    through the shape entry point (form 5) and the tuned device entry."""
+    torch = pytest.importorskip("torch")
+    sms = lib.tuning()["sms"]
+    n = 4 * sms * 32 * 2 + 13
+    h, cnt = workloads.poh_ragged(n=n, max_hashes=600, seed=71 + uniform)
+    if uniform:
+        cnt[:] = 600
+    cnt[:3] = [0, 1, 600]
+    exp = oracle.poh_verify_many(h, cnt, nthreads())
+    for shape in (True, False):
+        dh = torch.from_numpy(h.copy()).cuda()
+        dc = torch.from_numpy(cnt.astype(np.int64)).cuda()
+        ws = torch.empty(lib.poh_batch_workspace_size(len(cnt)), dtype=torch.uint8, device="cuda")
+        st = torch.cuda.current_stream().cuda_stream
+        if shape:
+            lib.poh_verify_batch_shape(dh, dc, ws, 4 * sms, lib.POH_AUTO, st)
+        else:
+            lib.poh_verify_batch_device(dh, dc, ws, st)
+        torch.cuda.synchronize()
+        assert np.array_equal(dh.cpu().numpy(), exp), shape
 
 
 def test_sig_batch_both_verify_modes(lib, oracle):
