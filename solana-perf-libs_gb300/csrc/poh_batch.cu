@@ -67,12 +67,25 @@ __global__ void poh_hist_kernel(const uint64_t* counts, uint64_t n, PohBatchScra
 // ~77.5 cycles per hash per sub-partition.  The shape with the smaller
 // makespan estimate runs (single warps only when 10 % shorter), as the host
 // forms decide from host counts.
-__global__ void poh_choose_kernel(PohBatchScratch* s, uint32_t sms) {
+//
+// Both persistent kernels are enqueued, paired first, and steered through
+// the queue rather than by a test in their code (an entry test in the
+// paired kernel cost 0.5 % on GB300, its code being that sensitive to
+// context): for single warps the queue head starts at n, so the paired
+// kernel finds the queue empty and ends, and poh_requeue_kernel then resets
+// it; for pairs the paired kernel drains the queue and the single-warp
+// kernel finds it empty.
+__global__ void poh_choose_kernel(PohBatchScratch* s, uint32_t sms, uint32_t n) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const double L = (double)s->longest, T = (double)s->total;
     const double pair = fmax(L * 1900.0, T * 1900.0 / (64.0 * sms));
     const double single = fmax(L * 2550.0, T * 77.5 / (4.0 * sms));
     s->choice = single < 0.9 * pair ? kChoseSingle : kChosePair;
+    if (s->choice == kChoseSingle) s->next = n;
+}
+
+__global__ void poh_requeue_kernel(PohBatchScratch* s) {
+    if (threadIdx.x == 0 && blockIdx.x == 0 && s->choice == kChoseSingle) s->next = 0;
 }
 
 // single warp: cursor[b] = number of entries in buckets above b (longest first)
@@ -131,7 +144,6 @@ static __device__ __noinline__ HashWords single_run(HashWords in, uint64_t r, ui
 template <int BW>
 __global__ void __launch_bounds__(32 * BW) poh_persistent_kernel(uint8_t* hashes, const uint64_t* counts, uint32_t n,
                                                                  PohBatchScratch* s, uint32_t one) {
-    if (s && s->choice == kChosePair) return;            // kPohAuto picked the other shape
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     uint64_t rem = 0;
@@ -374,7 +386,6 @@ template <int P>
 __global__ void __launch_bounds__(64 * P) poh_pair_persistent_kernel(uint8_t* hashes, const uint64_t* counts,
                                                                      uint32_t n, PohBatchScratch* s, uint32_t one) {
     static_assert(P >= 1 && P <= kMaxPairsPerBlock, "pairs per block");
-    if (s && s->choice == kChoseSingle) return;          // kPohAuto picked the other shape
     __shared__ uint64_t run_len[P];
     const uint32_t warp = threadIdx.x >> 5, pair = warp >> 1, role = warp & 1u;
     const uint32_t first = (blockIdx.x * P + pair) * 32u;   // direct mode only
@@ -408,16 +419,17 @@ cudaError_t launch_poh_batch(uint8_t* hashes, const uint64_t* counts, uint64_t n
     poh_scatter_kernel<<<blocks, 256, 0, s>>>(counts, n, sc);
     const uint64_t need = (n + 31) / 32;               // 32-lane groups
     if (form == kPohAuto) {
-        // both shapes are enqueued; the one not chosen exits at its first
-        // instruction.  Paired: `warps` as given; single: four warps per
-        // sub-partition, one per block.
+        // both shapes are enqueued (poh_choose_kernel); the one not chosen
+        // finds the queue empty.  Paired: `warps` as given; single: four
+        // warps per sub-partition, one per block.
         int dev = 0, sms = 0;
         if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
         if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-        poh_choose_kernel<<<1, 32, 0, s>>>(sc, (uint32_t)sms);
+        poh_choose_kernel<<<1, 32, 0, s>>>(sc, (uint32_t)sms, (uint32_t)n);
         const uint64_t pmax = warps / 2 > 0 ? (uint64_t)(warps / 2) : 1;
         const uint64_t pairs = need < pmax ? need : pmax;
         poh_pair_persistent_kernel<1><<<(unsigned)pairs, 64, 0, s>>>(hashes, counts, (uint32_t)n, sc, 1u);
+        poh_requeue_kernel<<<1, 32, 0, s>>>(sc);
         const uint64_t smax = 16ull * (uint64_t)sms;
         const uint64_t singles = need < smax ? need : smax;
         poh_persistent_kernel<1><<<(unsigned)singles, 32, 0, s>>>(hashes, counts, (uint32_t)n, sc, 1u);
