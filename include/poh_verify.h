@@ -46,7 +46,10 @@ size_t gb300_poh_batch_workspace_size(uint64_t num_elems);
 
 /* Device form: hashes (16-byte aligned), counts and workspace (at least
  * gb300_poh_batch_workspace_size bytes, 16-byte aligned) in GPU memory;
- * enqueued on `stream`. */
+ * enqueued on `stream`.  The launch shape (a schedule and a round warp per
+ * 32 chains, or one warp per 32 chains) is chosen on the GPU from the
+ * longest count and the sum of the counts, as gb300_poh_verify_batch
+ * chooses it on the host. */
 int gb300_poh_verify_batch_device(uint8_t* hashes, const uint64_t* num_hashes, uint64_t num_elems,
                                   void* workspace, size_t workspace_bytes, void* stream);
 
