@@ -345,3 +345,29 @@ def wire_packets(keypairs, sign, n: int = 4096, corrupt_frac: float = 0.05, malf
         kinds.append(kind)
         first += k
     return WirePackets(data, stride, plen, kinds)
+
+
+def fuzz_wire(w: WirePackets, seed: int):
+    """Copies of w's packets and lengths with, per packet, one of: every
+    byte random (the count byte often small), random bytes in the count and
+    message-header region (version, header, key count), or an edge data
+    length (0, 1, 2, 65, short by one, the stride, past the stride,
+    2^32 - 1).  Returns (data, lens)."""
+    rng = np.random.default_rng(seed)
+    data, lens = w.data.copy(), w.lens.copy()
+    n, stride = data.shape
+    for i in range(n):
+        r = rng.random()
+        if r < 0.25:
+            data[i] = rng.integers(0, 256, stride, dtype=np.uint8)
+            if rng.random() < 0.6:
+                data[i, 0] = rng.integers(1, 6)
+            lens[i] = rng.integers(0, stride + 1)
+        elif r < 0.65:
+            msg0 = 1 + 64 * int(data[i, 0])
+            for _ in range(int(rng.integers(1, 4))):
+                pos = int(rng.integers(0, 3)) if rng.random() < 0.3 else msg0 + int(rng.integers(0, 8))
+                data[i, min(pos, stride - 1)] = rng.integers(0, 256)
+        elif r < 0.8:
+            lens[i] = rng.choice([0, 1, 2, 65, max(0, int(lens[i]) - 1), stride, stride + 1, 0xffffffff])
+    return data, lens

@@ -114,3 +114,40 @@ def test_verify_packets_form_by_device_count(lib, oracle, n):
     assert counts.max() == 4
     out, got = lib.verify_packets(w.data, w.lens)
     assert np.array_equal(out, exp) and np.array_equal(got, counts)
+
+
+def _fuzzed(oracle, n, seed):
+    return workloads.fuzz_wire(_wire(oracle, n, seed, corrupt_frac=0.0, malformed_frac=0.0), seed)
+
+
+@pytest.mark.parametrize("seed", [201, 202])
+def test_extract_offsets_fuzzed(lib, oracle, seed):
+    """The device parse against the oracle's on fuzzed packets: per-packet
+    signature counts and the four per-signature arrays."""
+    torch = pytest.importorskip("torch")
+    data, lens = _fuzzed(oracle, 3000, seed)
+    counts, ml, ko, so, mo = oracle.wire_offsets(data, data.shape[1], lens)
+    assert (counts == 0).sum() > 300 and (counts > 0).sum() > 1000
+    n, stride = data.shape
+    cap = lib.packets_signature_capacity(n, stride)
+    d = torch.from_numpy(data.ravel().copy()).cuda()
+    dl = torch.from_numpy(lens.view(np.int32).copy()).cuda()
+    ws = torch.empty(lib.packets_workspace_size(n, stride), dtype=torch.uint8, device="cuda")
+    arrs = [torch.full((cap,), 0x7fffffff, dtype=torch.int32, device="cuda") for _ in range(4)]
+    dc = torch.zeros(n, dtype=torch.int32, device="cuda")
+    tot = torch.zeros(1, dtype=torch.int32, device="cuda")
+    lib.extract_offsets_device(d, stride, dl, ws, *arrs, counts=dc, total=tot,
+                               stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    t = int(tot.item())
+    assert t == counts.sum()
+    assert np.array_equal(dc.cpu().numpy().astype(np.uint32), counts)
+    for a, e in zip(arrs, (ml, ko, so, mo)):
+        assert np.array_equal(a[:t].cpu().numpy().view(np.uint32), e)
+
+
+def test_verify_packets_fuzzed(lib, oracle):
+    data, lens = _fuzzed(oracle, 2000, 203)
+    exp, _, counts = oracle.verify_wire_packets(data, data.shape[1], lens, nthreads())
+    out, got = lib.verify_packets(data, lens)
+    assert np.array_equal(out, exp) and np.array_equal(got, counts)

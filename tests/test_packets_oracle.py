@@ -118,3 +118,22 @@ def test_wire_generator_classes(oracle):
         else:
             assert v == 0, (i, kind)
     assert len(set(w.kinds)) >= 6
+
+
+def test_oracle_parse_matches_python_fuzzed(oracle):
+    """Fuzzed packets (random bytes, corrupted headers, edge lengths): the
+    oracle's C parse against the pure-Python one, packet by packet."""
+    w = workloads.wire_packets(oracle.create_keypairs, oracle.sign_packets, n=800, seed=301, corrupt_frac=0.0,
+                               malformed_frac=0.0)
+    data, lens = workloads.fuzz_wire(w, 301)
+    counts, so, ko, mo, ml = oracle.parse_packets(data, w.stride, lens)
+    parsed = 0
+    for i in range(len(lens)):
+        n = int(lens[i])
+        exp = (0,) if n > w.stride else py_parse(bytes(data[i, :n]))
+        assert counts[i] == exp[0], i
+        if exp[0]:
+            parsed += 1
+            base = i * w.stride
+            assert (so[i], ko[i], mo[i], ml[i]) == (base + exp[1], base + exp[2], base + exp[3], n - exp[3]), i
+    assert 200 < parsed < 700
