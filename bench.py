@@ -754,6 +754,7 @@ def bench_serving(lib, levels=(0.1, 0.25, 0.5, 0.8, 1.0, 1.2), duration_s=1.0, m
                 if dt > 0:
                     time.sleep(dt)
                 subs.append((kind, k) + tuple(submit(srv, kind, k)))
+            submit_rate = n / max(1e-9, time.perf_counter() - start)
             lat = {"v": [], "s": [], "p": []}
             t_first, t_last, sig_items = None, None, 0
             for kind, k, t, out in subs:
@@ -768,6 +769,7 @@ def bench_serving(lib, levels=(0.1, 0.25, 0.5, 0.8, 1.0, 1.2), duration_s=1.0, m
                 srv.release(t)
             sig_lat = lat["v"] + lat["s"]
             rows.append({"offered_fraction_of_peak": lv, "offered_requests_per_s": lam, "requests": n,
+                         "achieved_submit_rate": submit_rate,
                          "sig_items_per_s": sig_items / max(1e-9, (t_last - t_first) * 1e-9),
                          "sig_latency_ms": {"p50": _pct(sig_lat, 50) * 1e3, "p99": _pct(sig_lat, 99) * 1e3,
                                             "p99.9": _pct(sig_lat, 99.9) * 1e3},
