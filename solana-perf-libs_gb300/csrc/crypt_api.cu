@@ -146,6 +146,12 @@ bool init_locked() {
         bool ok = cudaStreamCreateWithFlags(&D.q[0].stream, cudaStreamNonBlocking) == cudaSuccess;
         if (ok) ok = crypt_tables_create(&D.tables, D.q[0].stream) == cudaSuccess;
         if (ok) ok = cudaDeviceGetAttribute(&D.sms, cudaDevAttrMultiProcessorCount, d) == cudaSuccess;
+        // every kernel of the library loaded now, not at its first launch
+        // (which may then wait for running kernels: see load_kernels)
+        if (ok)
+            ok = preload_verify_kernels() == cudaSuccess && preload_sign_kernels() == cudaSuccess &&
+                 preload_poh_kernels() == cudaSuccess && preload_poh_batch_kernels() == cudaSuccess &&
+                 preload_sig_batch_kernels() == cudaSuccess && preload_packets_kernels() == cudaSuccess;
         if (!ok) {
             fprintf(stderr, "libcuda-crypt: GPU %d unusable: %s\n", d, cudaGetErrorString(cudaGetLastError()));
             break;

@@ -23,6 +23,25 @@ struct SigBatch {
     int window = 4;               // verify: signed window width of h (4 or 5; the autotuner's choice)
 };
 
+// Kernels are loaded on the current device when these run, rather than at
+// their first launch.  Under lazy module loading (CUDA's default) a kernel's
+// first launch loads it, and that load can wait for unrelated kernels that
+// are running: in the served loop a first-used signature kernel waited up to
+// hundreds of ms for a PoH launch.  cudaFuncGetAttributes loads a function.
+template <class... K>
+inline cudaError_t load_kernels(K... k) {
+    cudaError_t e = cudaSuccess;
+    cudaFuncAttributes a;
+    ((e = (e == cudaSuccess ? cudaFuncGetAttributes(&a, k) : e)), ...);
+    return e;
+}
+cudaError_t preload_verify_kernels();
+cudaError_t preload_sign_kernels();
+cudaError_t preload_poh_kernels();
+cudaError_t preload_poh_batch_kernels();
+cudaError_t preload_sig_batch_kernels();
+cudaError_t preload_packets_kernels();
+
 // Ed25519 verify: out[i] = 1 if signature i is valid under the reference's
 // acceptance rules, else 0.  Forms: one thread per signature, or four lanes
 // per signature (lower latency on batches that do not fill the GPU).

@@ -242,6 +242,10 @@ cudaError_t enqueue_extract(const uint8_t* data, uint64_t stride, uint32_t n, co
 
 }  // namespace
 
+cudaError_t preload_packets_kernels() {
+    return load_kernels(parse_kernel, scan_local_kernel, scan_sums_kernel, expand_kernel, reduce_kernel);
+}
+
 size_t packets_workspace_size(uint32_t n, uint64_t stride) { return carve(nullptr, n, stride, nullptr); }
 
 uint64_t packets_signature_capacity(uint32_t n, uint64_t stride) { return (uint64_t)n * cap_per_packet(stride); }

@@ -59,6 +59,8 @@ __global__ void __launch_bounds__(POH_THREADS) poh_verify_kernel(uint8_t* hashes
 
 }  // namespace
 
+cudaError_t preload_poh_kernels() { return load_kernels(poh_verify_kernel); }
+
 cudaError_t launch_poh_verify(uint8_t* hashes, const uint64_t* num_hashes, uint64_t n, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     int dev = 0, sms = 0;

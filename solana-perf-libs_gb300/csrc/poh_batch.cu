@@ -395,6 +395,12 @@ __global__ void __launch_bounds__(64 * P) poh_pair_persistent_kernel(uint8_t* ha
 
 }  // namespace
 
+cudaError_t preload_poh_batch_kernels() {
+    return load_kernels(poh_hist_kernel, poh_scan_kernel, poh_scatter_kernel, poh_choose_kernel, poh_requeue_kernel,
+                        poh_persistent_kernel<1>, poh_persistent_kernel<4>, poh_pair_persistent_kernel<1>,
+                        poh_pair_persistent_kernel<2>);
+}
+
 size_t poh_batch_workspace_size(uint64_t n) { return sizeof(PohBatchScratch) + 4ull * (n ? n : 1); }
 
 cudaError_t launch_poh_pair_direct(uint8_t* hashes, const uint64_t* counts, uint64_t n, cudaStream_t s) {
@@ -511,6 +517,8 @@ extern "C" int gb300_poh_verify_batch_static(uint8_t* hashes, const uint64_t* nu
             if (e != cudaSuccess) return (int)e;
             int n = 0;
             e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+            if (e != cudaSuccess) return (int)e;
+            e = preload_poh_batch_kernels();           // loaded now, not at a later first launch
             if (e != cudaSuccess) return (int)e;
             g_static_sms[dev] = n > 0 ? n : 1;
             g_static_ptr[dev] = p;

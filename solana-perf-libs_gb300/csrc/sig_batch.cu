@@ -116,6 +116,13 @@ cudaError_t launch_t(const SigWork& w, int blocks_per_sm, int sms, cudaStream_t 
 
 }  // namespace
 
+cudaError_t preload_sig_batch_kernels() {
+    return load_kernels(sig_persistent_kernel<64, 4, 1>, sig_persistent_kernel<64, 5, 1>,
+                        sig_persistent_kernel<128, 4, 1>, sig_persistent_kernel<128, 5, 1>,
+                        sig_persistent_kernel<128, 4, 3>, sig_persistent_kernel<256, 4, 1>,
+                        sig_persistent_kernel<256, 5, 1>);
+}
+
 // Verify signatures four lanes each while the batch leaves the GPU idle
 // (the same size rule as launch_ed25519_verify: up to 64 per SM).
 cudaError_t launch_sig_batch(const SigWork& w_in, int threads, int blocks_per_sm, int sms, cudaStream_t s) {

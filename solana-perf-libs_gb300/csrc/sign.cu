@@ -73,6 +73,8 @@ __global__ void ed25519_keypair_kernel(const uint8_t* seeds, uint8_t* pk_out, ui
 
 }  // namespace
 
+cudaError_t preload_sign_kernels() { return load_kernels(ed25519_sign_kernel, ed25519_keypair_kernel); }
+
 cudaError_t launch_ed25519_sign(const SigBatch& b, cudaStream_t s) {
     if (b.n == 0) return cudaSuccess;
     ed25519_sign_kernel<<<(b.n + SIGN_THREADS - 1) / SIGN_THREADS, SIGN_THREADS, kCombBytes, s>>>(b);

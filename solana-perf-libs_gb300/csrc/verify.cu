@@ -82,6 +82,12 @@ __global__ void check_small_order_kernel(const uint8_t* pts, uint8_t* out, uint3
 
 }  // namespace
 
+cudaError_t preload_verify_kernels() {
+    return load_kernels(ed25519_verify_kernel<4, VERIFY_MIN_BLOCKS>, ed25519_verify_kernel<4, 4>,
+                        ed25519_verify_kernel<5, VERIFY_MIN_BLOCKS>, ed25519_verify_quad_kernel,
+                        check_small_order_kernel);
+}
+
 cudaError_t launch_ed25519_verify_form(const SigBatch& b, cudaStream_t s, int form) {
     if (b.n == 0) return cudaSuccess;
     if (form == kVerifyQuad) {
