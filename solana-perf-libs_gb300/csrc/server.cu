@@ -404,11 +404,14 @@ void dispatcher(gb300_server* sv) {
             while (!sv->pending_sig.empty()) {
                 const Req& r = sv->pending_sig.front();
                 // merge while the launch fits the item cap, the memory budget
-                // and the slot's resident packet ring (no reallocation); one
-                // launch holds wire packets of one stride or offset jobs
+                // and the slot's resident packet ring (no reallocation; and
+                // below 4 GiB, the reach of 32-bit packet offsets, should a
+                // large request have grown the ring); one launch holds wire
+                // packets of one stride or offset jobs
+                const uint64_t ring = S.d_data.cap < 0xfffffff0ull ? S.d_data.cap : 0xfffffff0ull;
                 if (!S.reqs.empty() && ((r.kind == 3) != wire || (wire && r.stride != stride) ||
                                         items + r.n > sv->max_items || sv->in_use + bytes + r.bytes > sv->cap ||
-                                        pkt + r.ring_bytes + 16 > S.d_data.cap))
+                                        pkt + r.ring_bytes + 16 > ring))
                     break;
                 if (S.reqs.empty() && sv->in_use + r.bytes > sv->cap) break;   // wait for memory
                 items += r.n;
