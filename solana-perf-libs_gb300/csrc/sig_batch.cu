@@ -98,10 +98,17 @@ cudaError_t launch_t(const SigWork& w, int blocks_per_sm, int sms, cudaStream_t 
         opted.fetch_or(bit);
     }
     const size_t dyn = w.s.n > 0 ? kCombBytes : 0;
-    int maxb = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, sig_persistent_kernel<T, W, MINB>, T, dyn);
-    if (e != cudaSuccess) return e;
-    if (maxb < 1) maxb = 1;
+    // resident blocks per SM, per device and with or without the comb: the
+    // occupancy query costs host time on every launch otherwise
+    static std::atomic<int> occ[64][2];
+    std::atomic<int>& slot = occ[dev & 63][dyn ? 1 : 0];
+    int maxb = slot.load();
+    if (maxb == 0) {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, sig_persistent_kernel<T, W, MINB>, T, dyn);
+        if (e != cudaSuccess) return e;
+        if (maxb < 1) maxb = 1;
+        slot.store(maxb);
+    }
     int b = blocks_per_sm < 1 ? maxb : (blocks_per_sm < maxb ? blocks_per_sm : maxb);
     // (a launch that may take the four-lane form by its device count is
     // sized for it)
