@@ -42,7 +42,7 @@ def _verify_items(oracle, seed):
 
 def test_verify_long_messages_every_form(lib, oracle):
     items = _verify_items(oracle, 401)
-    sp = pack_items(items, gap_seed=9)
+    sp = pack_items(items, gap_seed=9, elems_split=3)     # 5.6 MB in three runs: the parallel staging copy
     exp = oracle.verify_packets(sp, nthreads())
     assert exp.sum() == len(LENGTHS)                       # the signed messages, none of the altered ones
     assert np.array_equal(lib.verify_many(sp), exp)

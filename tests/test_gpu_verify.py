@@ -171,3 +171,36 @@ def test_verify_device_form(lib, oracle):
     lib.verify_device(pk, lens, po, so, mo, out, torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
     assert np.array_equal(out.cpu().numpy(), exp)
+
+
+@pytest.mark.parametrize("register", [False, True])
+def test_verify_and_sign_with_empty_runs(lib, oracle, register):
+    """gpu_Elems runs with empty ones between them (num = 0), from pageable
+    buffers and from buffers page-locked with cuda_host_register (copied run
+    by run straight from the caller's memory)."""
+    from test_gpu_sign import _sign_items
+    rng = np.random.default_rng(47)
+    pk, sk = oracle.create_keypairs(rng.integers(0, 256, (90, 32), dtype=np.uint8))
+    items = []
+    for i in range(90):
+        msg = rng.bytes(int(rng.integers(0, 200)))
+        sig = oracle.sign(msg, bytes(pk[i]), bytes(sk[i]))
+        if i % 7 == 3:
+            sig = sig[:5] + bytes([sig[5] ^ 1]) + sig[6:]
+        items.append((sig, msg, bytes(pk[i])))
+    sp = pack_items(items, gap_seed=12, elems_split=3)
+    empty = np.zeros(0, dtype=np.uint8)
+    sp.batches = [empty, sp.batches[0], empty, empty, sp.batches[1], sp.batches[2], empty]
+    ssp = _sign_items([(rng.bytes(int(rng.integers(0, 150))), bytes(pk[i]), bytes(sk[i])) for i in range(40)])
+    flat = ssp.batches[0]
+    cut = (len(flat) // ssp.message_size // 2) * ssp.message_size
+    ssp.batches = [flat[:cut].copy(), empty, flat[cut:].copy()]
+    regs = [b for b in sp.batches + ssp.batches if b.nbytes] if register else []
+    for b in regs:
+        assert lib.host_register(b) == 0
+    try:
+        assert np.array_equal(lib.verify_many(sp), oracle.verify_packets(sp, nthreads()))
+        assert np.array_equal(lib.sign_many(ssp), oracle.sign_packets(ssp, nthreads()))
+    finally:
+        for b in regs:
+            lib.host_unregister(b)
