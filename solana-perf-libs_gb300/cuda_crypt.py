@@ -422,6 +422,8 @@ class Server:
         L.gb300_server_submit_packets.argtypes = [ctypes.c_void_p, ctypes.POINTER(GpuElems), ctypes.c_uint32,
                                                   ctypes.c_uint32, _u32p, _u8p, _u32p]
         L.gb300_server_submit_packets.restype = ctypes.c_uint64
+        L.gb300_server_trace.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]
+        L.gb300_server_trace.restype = ctypes.c_int
         cfg = ServerConfig(device_memory_cap, sig_slots, poh_slots, max_items_per_launch)
         self.h = L.gb300_server_create(ctypes.byref(cfg))
         if not self.h:
@@ -509,8 +511,6 @@ class Server:
         """Recent launches: [kind, requests, items, admitted_ns, enqueued_ns,
         completed_ns, copy_in_ms, kernels_ms, copy_out_ms] each."""
         import json
-        self.L.gb300_server_trace.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]
-        self.L.gb300_server_trace.restype = ctypes.c_int
         buf = ctypes.create_string_buffer(1 << 22)
         n = self.L.gb300_server_trace(self.h, buf, len(buf))
         return json.loads(buf.value[:n].decode()) if n else []
