@@ -93,6 +93,23 @@ def test_vs_ref_sign_verify(oracle, ref):
             assert oracle.verify(bytes(s2), m, pk) == ref.verify(bytes(s2), m, pk)
 
 
+def test_vs_ref_long_messages(oracle, ref):
+    """Messages far past a packet (many SHA-512 blocks): sign, verify, and
+    verify with a late or middle byte altered, against the reference."""
+    rng = np.random.default_rng(71)
+    for n in (1232, 1233, 2047, 4103, 65647, 200003):
+        seed = bytes(rng.integers(0, 256, 32, dtype=np.uint8).tolist())
+        pk, sk = oracle.create_keypair(seed)
+        m = rng.bytes(n)
+        s = oracle.sign(m, pk, sk)
+        assert s == ref.sign(m, pk, sk), n
+        assert oracle.verify(s, m, pk) == ref.verify(s, m, pk) == 1, n
+        for pos in (n - 1, n // 2):
+            bad = bytearray(m)
+            bad[pos] ^= 0x40
+            assert oracle.verify(s, bytes(bad), pk) == ref.verify(s, bytes(bad), pk) == 0, (n, pos)
+
+
 def test_vs_ref_decoding(oracle, ref):
     rng = np.random.default_rng(8)
     for _ in range(20000):
