@@ -61,7 +61,10 @@ int gb300_poh_verify_batch_device(uint8_t* hashes, const uint64_t* num_hashes, u
  * a 1 MiB array built into the library, so at most 262,144 entries per call
  * (more returns cudaErrorInvalidValue with a message on stderr).  The first
  * call on each device looks up that array's device address; make that first
- * call before any stream capture.  All calls share the one array, so calls
+ * call before any stream capture.  The address is kept for the life of the
+ * process and belongs to the device's primary context (the one the CUDA
+ * runtime uses): do not call it from another context, nor after
+ * cudaDeviceReset.  All calls share the one array, so calls
  * that overlap on the GPU (concurrent streams or threads) race: serialise
  * them.  hashes 16-byte and counts 8-byte aligned; enqueued on `stream`;
  * returns 0 or a cudaError_t. */

@@ -27,9 +27,11 @@ def build_oracle() -> None:
     subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
 
 
-def build_ref(ref_root: str = "/root/reference") -> bool:
+def build_ref(ref_root: str | None = None) -> bool:
     """Compile the reference's host code from its own sources when the tree is
-    present (x86_64 only).  Returns True when oracle/_ref is usable."""
+    present (x86_64 only).  The tree is `ref_root`, else $REF_ROOT, else
+    /root/reference.  Returns True when oracle/_ref is usable."""
+    ref_root = ref_root or os.environ.get("REF_ROOT", "/root/reference")
     if os.path.exists(REF_SO):
         return True
     if not os.path.isdir(ref_root):

@@ -35,6 +35,7 @@
 #include "tables.cuh"
 #include "host_buffers.h"
 #include "host_copy.h"
+#include "queue_pick.h"
 
 #include <functional>
 
@@ -106,7 +107,6 @@ struct Device {
     int sms = 0;
     CurveTables* tables = nullptr;
     Queue q[kQueues];
-    uint32_t next_queue = 0;
     std::once_flag tuned;
     std::atomic<bool> tuned_done{false};
     Tuning tune;
@@ -115,7 +115,7 @@ struct Device {
 std::mutex g_mu;
 int g_num_gpus = -1;  // -1: not initialised yet
 Device g_dev[kMaxGpus];
-uint32_t g_next_gpu = 0;
+gb300::QueueTurns<kMaxGpus> g_turns;     // round-robin state, under g_mu
 
 // Streams beyond CUDA_DEVICE_MAX_CONNECTIONS (default 8) share hardware work
 // queues, so a short verify launch can end up queued behind a second-long
@@ -173,27 +173,21 @@ struct Lease {
 };
 
 // GPU round-robin, then the GPU's first idle queue (the next one in turn
-// when all are busy), then the queue's lock (reference gpu_ctx.cu:46-73
-// picks the next queue in turn every time: a caller issuing one call after
-// another then meets every queue's first-use buffer growth and graph
-// capture; measured on GB300 for 131 MB ragged batches: 15.4 ms per call
-// in turn against 9.2 ms on the warm queue).
+// when all are busy), then the queue's lock: gb300::pick_queue
+// (queue_pick.h).  The reference (gpu_ctx.cu:46-73) picks the next queue in
+// turn every time: a caller issuing one call after another then meets every
+// queue's first-use buffer growth and graph capture; measured on GB300 for
+// 131 MB ragged batches: 15.4 ms per call in turn against 9.2 ms on the
+// warm queue.
 bool acquire(Lease& L) {
     std::unique_lock<std::mutex> lk(g_mu);
     if (!init_locked()) return false;
-    Device& D = g_dev[g_next_gpu % (uint32_t)g_num_gpus];
-    g_next_gpu++;
-    Queue* pick = nullptr;
-    for (int k = 0; k < kQueues && !pick; k++)
-        if (D.q[k].mu.try_lock()) pick = &D.q[k];        // non-blocking under g_mu
-    const bool held = pick != nullptr;
-    if (!held) {
-        pick = &D.q[D.next_queue % kQueues];
-        D.next_queue++;
-    }
+    const gb300::QueuePick p = gb300::pick_queue(
+        g_turns, g_num_gpus, kQueues, [](int g, int k) { return g_dev[g].q[k].mu.try_lock(); });
     lk.unlock();
-    Queue& Q = *pick;
-    if (!held) Q.mu.lock();
+    Device& D = g_dev[p.gpu];
+    Queue& Q = D.q[p.queue];
+    if (!p.held) Q.mu.lock();
     L.dev = &D;
     L.q = &Q;
     cudaSetDevice(D.id);

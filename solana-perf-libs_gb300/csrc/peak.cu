@@ -7,6 +7,12 @@
 //   kind 1: mad.wide.u32        (32x32 -> 64-bit multiply-add)
 //   kind 2: mad.lo.u32          (32-bit multiply-add)
 //   kind 3: shf.r.wrap.b32      (funnel shift / rotate)
+//   kind 4: the SHA-256 mix: per 16 ops, 8 lop3.b32 + 4 shf.r.wrap.b32 (ALU
+//           pipe) + 4 mad.lo.u32 (multiply pipe).  A SHA-256 compression
+//           counted by the 1,384-op convention is 1,024 logic/shift ops and
+//           360 additions; additions can issue on either pipe, so 3 : 1
+//           ALU : multiply is the mix a warp can spread over both pipes, and
+//           its rate is the ceiling of that instruction mix.
 // The operands of every op come from two other evolving chains, so no two
 // consecutive ops on a chain can be merged into one.
 #include <cuda_runtime.h>
@@ -39,9 +45,17 @@ __global__ void __launch_bounds__(256) int_peak_kernel(uint32_t* sink, uint32_t 
                 uint32_t r;
                 asm volatile("mad.lo.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a[k]), "r"(a[(k + 5) & 15]), "r"(a[(k + 11) & 15]));
                 a[k] = r;
-            } else {
+            } else if (KIND == 3 || (KIND == 4 && (k & 3) == 1)) {
                 uint32_t r;
                 asm volatile("shf.r.wrap.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(a[k]), "r"(a[(k + 5) & 15]), "r"(a[(k + 11) & 15]));
+                a[k] = r;
+            } else if ((k & 3) == 3) {     // KIND 4: every fourth op on the multiply pipe
+                uint32_t r;
+                asm volatile("mad.lo.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a[k]), "r"(a[(k + 5) & 15]), "r"(a[(k + 11) & 15]));
+                a[k] = r;
+            } else {                       // KIND 4: lop3 (k & 3 == 0 or 2)
+                uint32_t r;
+                asm volatile("lop3.b32 %0, %1, %2, %3, 0x96;" : "=r"(r) : "r"(a[k]), "r"(a[(k + 5) & 15]), "r"(a[(k + 11) & 15]));
                 a[k] = r;
             }
         }
@@ -63,6 +77,7 @@ extern "C" int gb300_int_peak_launch(int kind, uint32_t blocks, uint32_t threads
         case 1: int_peak_kernel<1><<<blocks, threads, 0, s>>>(sink, iters, 12345u); break;
         case 2: int_peak_kernel<2><<<blocks, threads, 0, s>>>(sink, iters, 12345u); break;
         case 3: int_peak_kernel<3><<<blocks, threads, 0, s>>>(sink, iters, 12345u); break;
+        case 4: int_peak_kernel<4><<<blocks, threads, 0, s>>>(sink, iters, 12345u); break;
         default: return (int)cudaErrorInvalidValue;
     }
     return (int)cudaGetLastError();

@@ -142,3 +142,35 @@ def test_vs_ref_poh(oracle, ref):
     for n in [0, 1, 2, 17, 1000]:
         h = bytes(rng.integers(0, 256, 32, dtype=np.uint8).tolist())
         assert oracle.poh_chain(h, n) == ref.poh_chain(h, n)
+
+
+def _digest(*arrays) -> str:
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def test_oracle_matches_reference_config_digests(oracle):
+    """The full-size workload digests (made by the reference's host code)
+    reproduced by the oracle: the 1,024-packet verify, 4096 x 12,500 PoH and
+    the 64-batch ragged verify + 359 signing jobs.  The 16,384-chain ragged
+    PoH (1.17 G hashes) is checked on the GPU only."""
+    import json
+    import workloads
+    from conftest import GOLDEN
+    with open(os.path.join(GOLDEN, "config_digests.json")) as f:
+        g = json.load(f)
+    n = os.cpu_count() or 1
+    sp, _ = workloads.verify_uniform(oracle.create_keypairs, oracle.sign_packets, n=1024, seed=1)
+    assert _digest(sp.concatenated()) == g["verify_1024"]["input_sha256"]
+    assert _digest(oracle.verify_packets(sp, n)) == g["verify_1024"]["verdicts_sha256"]
+    h, c = workloads.poh_uniform(4096, 12500, seed=2)
+    assert _digest(oracle.poh_verify_many(h, c, n)) == g["poh_uniform"]["final_sha256"]
+    rs = workloads.ragged_sigs(oracle.create_keypairs, oracle.sign_packets, seed=3)
+    gr = g["ragged_sigs"]
+    assert _digest(*[s.concatenated() for s in rs.verify]) == gr["verify_input_sha256"]
+    assert _digest(np.concatenate([oracle.verify_packets(s, n) for s in rs.verify])) == gr["verdicts_sha256"]
+    assert _digest(*[oracle.sign_packets(s, n) for s in rs.sign]) == gr["signatures_sha256"]
+    h, c = workloads.poh_ragged(16384, 1_000_000, seed=4)
+    assert _digest(h, c) == g["poh_ragged"]["input_sha256"]
