@@ -16,7 +16,9 @@ extern "C" {
 /* Launches blocks x threads (threads <= 256) threads, each running iters
  * rounds of 16 dependent-chain ops of one form:
  *   kind 0 lop3.b32, 1 mad.wide.u32, 2 mad.lo.u32, 3 shf.r.wrap.b32,
- *   4 the SHA-256 mix: 8 lop3.b32 + 4 shf.r.wrap.b32 + 4 mad.lo.u32 per 16.
+ *   4 the SHA-256 proportions: 8 lop3.b32 + 4 shf.r.wrap.b32 + 4 mad.lo.u32
+ *   per 16, 5 the fastest measured mix: 4 lop3.b32 + 4 shf.r.wrap.b32 +
+ *   8 add.u32 per 16.
  * Executed ops = blocks * threads * iters * 16.  `sink` is a device word
  * the kernel may write.  Enqueued on `stream`; returns a cudaError_t. */
 int gb300_int_peak_launch(int kind, uint32_t blocks, uint32_t threads, uint32_t iters, uint32_t* sink,

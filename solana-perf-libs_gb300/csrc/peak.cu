@@ -7,12 +7,14 @@
 //   kind 1: mad.wide.u32        (32x32 -> 64-bit multiply-add)
 //   kind 2: mad.lo.u32          (32-bit multiply-add)
 //   kind 3: shf.r.wrap.b32      (funnel shift / rotate)
-//   kind 4: the SHA-256 mix: per 16 ops, 8 lop3.b32 + 4 shf.r.wrap.b32 (ALU
-//           pipe) + 4 mad.lo.u32 (multiply pipe).  A SHA-256 compression
-//           counted by the 1,384-op convention is 1,024 logic/shift ops and
-//           360 additions; additions can issue on either pipe, so 3 : 1
-//           ALU : multiply is the mix a warp can spread over both pipes, and
-//           its rate is the ceiling of that instruction mix.
+//   kind 4: per 16 ops, 8 lop3.b32 + 4 shf.r.wrap.b32 + 4 mad.lo.u32: the
+//           SHA-256 proportions (a compression counted by the 1,384-op
+//           convention is 1,024 logic/shift ops and 360 additions) with the
+//           additions on the multiply pipe.
+//   kind 5: per 16 ops, 4 lop3.b32 + 4 shf.r.wrap.b32 + 8 add.u32: the
+//           fastest mix of these instruction forms measured on GB300
+//           (27.2 Tops/s against 18.8 for lop3 alone and 20.1 for kind 4),
+//           i.e. the integer issue ceiling the roofline divides by.
 // The operands of every op come from two other evolving chains, so no two
 // consecutive ops on a chain can be merged into one.
 #include <cuda_runtime.h>
@@ -45,15 +47,19 @@ __global__ void __launch_bounds__(256) int_peak_kernel(uint32_t* sink, uint32_t 
                 uint32_t r;
                 asm volatile("mad.lo.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a[k]), "r"(a[(k + 5) & 15]), "r"(a[(k + 11) & 15]));
                 a[k] = r;
-            } else if (KIND == 3 || (KIND == 4 && (k & 3) == 1)) {
+            } else if (KIND == 5 && (k & 1)) {     // KIND 5: every other op an addition
+                uint32_t r;
+                asm volatile("add.u32 %0, %1, %2;" : "=r"(r) : "r"(a[k]), "r"(a[(k + 5) & 15]));
+                a[k] = r;
+            } else if (KIND == 3 || (KIND == 4 && (k & 3) == 1) || (KIND == 5 && (k & 2))) {
                 uint32_t r;
                 asm volatile("shf.r.wrap.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(a[k]), "r"(a[(k + 5) & 15]), "r"(a[(k + 11) & 15]));
                 a[k] = r;
-            } else if ((k & 3) == 3) {     // KIND 4: every fourth op on the multiply pipe
+            } else if (KIND == 4 && (k & 3) == 3) {     // KIND 4: every fourth op on the multiply pipe
                 uint32_t r;
                 asm volatile("mad.lo.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a[k]), "r"(a[(k + 5) & 15]), "r"(a[(k + 11) & 15]));
                 a[k] = r;
-            } else {                       // KIND 4: lop3 (k & 3 == 0 or 2)
+            } else {                       // KIND 4 (k & 3 == 0 or 2) and KIND 5 (k & 3 == 0): lop3
                 uint32_t r;
                 asm volatile("lop3.b32 %0, %1, %2, %3, 0x96;" : "=r"(r) : "r"(a[k]), "r"(a[(k + 5) & 15]), "r"(a[(k + 11) & 15]));
                 a[k] = r;
@@ -78,6 +84,7 @@ extern "C" int gb300_int_peak_launch(int kind, uint32_t blocks, uint32_t threads
         case 2: int_peak_kernel<2><<<blocks, threads, 0, s>>>(sink, iters, 12345u); break;
         case 3: int_peak_kernel<3><<<blocks, threads, 0, s>>>(sink, iters, 12345u); break;
         case 4: int_peak_kernel<4><<<blocks, threads, 0, s>>>(sink, iters, 12345u); break;
+        case 5: int_peak_kernel<5><<<blocks, threads, 0, s>>>(sink, iters, 12345u); break;
         default: return (int)cudaErrorInvalidValue;
     }
     return (int)cudaGetLastError();
