@@ -4,13 +4,26 @@
  *
  * A server owns one GPU (the device current at creation) and a dispatcher
  * thread.  Requests -- an Ed25519 verify or sign job, a batch of Solana
- * wire-format packets, or a PoH batch -- are queued by any thread and admitted as launch slots and device memory free
- * up (device memory held by in-flight requests stays below the configured
- * cap).  Signature requests that arrive while earlier ones are on the GPU
- * are merged into the next persistent launch (continuous batching) on
- * high-priority streams; PoH requests run on a low-priority stream so a long
- * chain does not hold up signature work.  Each request's results are exactly
- * those of the corresponding one-call entry point.
+ * wire-format packets, or a PoH batch -- are queued by any thread and
+ * admitted as GPU capacity and device memory free up (device memory held by
+ * in-flight requests stays below the configured cap).
+ *
+ * Verify and sign jobs go by default (sig_mode 0) to a resident signature
+ * service: the submitting thread stages the job into rings allocated when
+ * the server is created and publishes it, in 32-signature chunks (8 when
+ * the verifies in flight leave the GPU idle, four lanes each), to the FIFO of
+ * one long-lived kernel on a high-priority stream; each job completes as
+ * soon as its own chunks are done, whatever else is in flight, and the
+ * kernel leaves after 20 ms without work (launched again on demand;
+ * GB300_CRYPT_SERVER_IDLE_US changes the wait).  Jobs too large for the
+ * rings (1 GiB of device inputs at most, bounded by the memory cap; 256 MiB
+ * of pageable packets; 64 MiB of results; 2^18 chunks) take the slot path.
+ * With sig_mode 1, and always for wire-format packet batches, requests that
+ * arrive while earlier ones are on the GPU are merged into the next
+ * persistent launch of a slot (continuous batching) on high-priority
+ * streams.  PoH requests run on a low-priority stream so a long chain does
+ * not hold up signature work.  Each request's results are exactly those of
+ * the corresponding one-call entry point.
  *
  * The caller's buffers must stay valid, and its outputs untouched, until
  * the request is complete.  Page-locked (cuda_host_register) packet buffers
@@ -31,10 +44,13 @@ typedef struct gb300_server gb300_server;
 
 typedef struct {
     uint64_t device_memory_cap;      /* bytes in flight on the GPU; 0 = 8 GiB */
-    uint32_t sig_slots;              /* concurrent signature launches; 0 = 3 */
+    uint32_t sig_slots;              /* concurrent signature launches; 0 = 3 (2 beside
+                                        the signature service) */
     uint32_t poh_slots;              /* concurrent PoH launches; 0 = 2 */
     uint32_t max_items_per_launch;   /* signatures merged into one launch; 0 = 65536
                                         (a larger request runs alone) */
+    uint32_t sig_mode;               /* verify/sign jobs: 0 = resident signature service,
+                                        1 = merged launches on the slots */
 } gb300_server_config;
 
 /* Creates a server on the current device (cfg may be NULL); NULL on failure. */
@@ -82,7 +98,13 @@ int gb300_server_times(gb300_server* s, uint64_t ticket, int64_t* submit_ns, int
  *  admitted_ns, enqueued_ns, completed_ns, copy_in_ms, kernels_ms,
  *  copy_out_ms]: host times of the launch, then the GPU time of its input
  * copies, its kernels and its result copy (CUDA events; -1 after a
- * failure); returns the length written. */
+ * failure).  A job served by the resident signature service appears as
+ * [4, 1, items, submitted_ns, published_ns, completed_ns, wait_ms, run_ms,
+ * total_ms]: ms from its publication to the GPU's first claim of one of its
+ * chunks, from that claim to its completion on the GPU (GPU clock, related
+ * to the host clock at server creation; -1 after a failure), and from
+ * publication to completion as the host saw it.  Returns the length
+ * written. */
 int gb300_server_trace(gb300_server* s, char* buf, size_t len);
 
 /* Counters as a JSON object; returns the length written. */

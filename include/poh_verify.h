@@ -70,6 +70,54 @@ int gb300_poh_verify_batch_device(uint8_t* hashes, const uint64_t* num_hashes, u
  * returns 0 or a cudaError_t. */
 int gb300_poh_verify_batch_static(uint8_t* hashes, const uint64_t* num_hashes, uint64_t num_elems, void* stream);
 
+/* ---- Solana ledger entries: PoH chains with transaction mixins ---------
+ * No counterpart in the reference library: its caller (Solana's ledger-entry
+ * verification) runs each entry's plain hashes through poh_verify_many and
+ * finishes the entry on the host.  These entry points do the whole entry on
+ * the GPU.  From its start hash h (the previous entry's hash) an entry of
+ * num_hashes hashes ends at
+ *   no mixin (a tick):      h <- SHA-256(h), num_hashes times;
+ *   mixin m (32 bytes, the hash of the entry's transactions):
+ *                           h <- SHA-256(h), max(num_hashes, 1) - 1 times,
+ *                           then h <- SHA-256(h || m).
+ * All 32-byte arrays are n * 32 bytes, entry i at offset 32 i. */
+
+/* Device memory the device form of entry verification needs for n entries. */
+size_t gb300_poh_entries_workspace_size(uint64_t num_entries);
+
+/* ok[i] = 1 iff entry i, started from start_hashes[i], ends at expected[i]
+ * (has_mixin[i] != 0: mixins[i] is its mixin; otherwise mixins[i] is not
+ * read); out_hashes[i] (nullable) receives the computed hash.  Device
+ * pointers, 32-byte arrays and the workspace 16-byte aligned, counts 8-byte
+ * aligned; enqueued on `stream`; returns a cudaError_t.  The plain hashes of
+ * all entries run as one ragged persistent PoH batch (longest first). */
+int gb300_poh_verify_entries_device(const uint8_t* start_hashes, const uint64_t* num_hashes, const uint8_t* mixins,
+                                    const uint8_t* has_mixin, const uint8_t* expected, uint64_t num_entries,
+                                    uint8_t* ok, uint8_t* out_hashes, void* workspace, size_t workspace_bytes,
+                                    void* stream);
+
+/* Host form of gb300_poh_verify_entries_device (host buffers, synchronous);
+ * returns 0, 1 when no GPU is present, or a cudaError_t. */
+int gb300_poh_verify_entries(const uint8_t* start_hashes, const uint64_t* num_hashes, const uint8_t* mixins,
+                             const uint8_t* has_mixin, const uint8_t* expected, size_t num_entries, uint8_t* ok);
+
+/* Recording: chain c starts from hashes[c] and runs entries first[c] ..
+ * first[c + 1] - 1 in order (first has num_chains + 1 elements, first[0] = 0,
+ * non-decreasing, first[num_chains] = num_entries); entry e's hash goes to
+ * entry_hashes[e] and hashes[c] ends as chain c's last hash.  Entries at or
+ * past num_entries are never read.  Entries of one chain are serial, so the
+ * GPU records many chains at once, one thread each.  Device pointers
+ * (32-byte arrays 16-byte aligned), enqueued on `stream`; returns a
+ * cudaError_t. */
+int gb300_poh_record_device(uint8_t* hashes, uint64_t num_chains, const uint64_t* first, uint64_t num_entries,
+                            const uint64_t* num_hashes, const uint8_t* mixins, const uint8_t* has_mixin,
+                            uint8_t* entry_hashes, void* stream);
+
+/* Host form of gb300_poh_record_device (host buffers, synchronous); returns
+ * 0, 1 when no GPU is present, or a cudaError_t. */
+int gb300_poh_record(uint8_t* hashes, size_t num_chains, const uint64_t* first, const uint64_t* num_hashes,
+                     const uint8_t* mixins, const uint8_t* has_mixin, uint8_t* entry_hashes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -957,6 +957,90 @@ void oracle_poh_verify_many(u8 *hashes, const u64 *num_hashes, size_t n, int nth
     run_jobs(j, nthreads);
 }
 
+/* ---- PoH entries with transaction mixins ---------------------------------
+ * Not part of the reference: poh_verify_many (poh_verify.cu:80-144) only
+ * iterates SHA-256; its caller, Solana's ledger-entry verification, feeds it
+ * each entry's start hash and a hash count and finishes every entry on the
+ * host.  This restates that entry rule from Solana's published ledger format
+ * as the checker of the library's on-device form; there is no reference code
+ * or fixture for it, so parity is pinned to FIPS SHA-256 (hashlib) and the
+ * rule below, not to the reference.
+ *
+ * An entry is (num_hashes, optional 32-byte mixin = the hash of its
+ * transactions).  From the start hash h (the previous entry's hash):
+ *   no mixin (a tick):  h <- SHA-256(h), num_hashes times;
+ *   mixin m:            h <- SHA-256(h), max(num_hashes, 1) - 1 times, then
+ *                       h <- SHA-256(h || m) (64 bytes: two compressions).
+ * The result is the entry's hash. */
+static void poh_mix_step(u8 hash[32], const u8 mixin[32]) {
+    u8 msg[64];
+    memcpy(msg, hash, 32);
+    memcpy(msg + 32, mixin, 32);
+    oracle_sha256(msg, 64, hash);
+}
+
+void oracle_poh_entry(u8 hash[32], u64 num_hashes, const u8 *mixin) {
+    if (!mixin) {
+        oracle_poh_chain(hash, num_hashes);
+        return;
+    }
+    oracle_poh_chain(hash, num_hashes ? num_hashes - 1 : 0);
+    poh_mix_step(hash, mixin);
+}
+
+/* Entry i starts from start_hashes[i]; ok[i] = 1 iff its hash equals
+ * expected[i]; the computed hash goes to out_hashes[i] (nullable).  Entries
+ * spread over nthreads host threads. */
+typedef struct {
+    const u8 *start, *mixins, *has_mixin, *expected;
+    const u64 *num_hashes;
+    u8 *ok, *out;
+    size_t begin, end;
+} entries_job_t;
+
+static void *entries_run(void *arg) {
+    entries_job_t *j = (entries_job_t *)arg;
+    for (size_t i = j->begin; i < j->end; i++) {
+        u8 h[32];
+        memcpy(h, j->start + 32 * i, 32);
+        oracle_poh_entry(h, j->num_hashes[i], j->has_mixin[i] ? j->mixins + 32 * i : NULL);
+        j->ok[i] = memcmp(h, j->expected + 32 * i, 32) == 0;
+        if (j->out) memcpy(j->out + 32 * i, h, 32);
+    }
+    return NULL;
+}
+
+void oracle_poh_verify_entries(const u8 *start_hashes, const u64 *num_hashes, const u8 *mixins, const u8 *has_mixin,
+                               const u8 *expected, size_t n, u8 *ok, u8 *out_hashes, int nthreads) {
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    if ((size_t)nthreads > n) nthreads = n ? (int)n : 1;
+    pthread_t th[256];
+    entries_job_t jobs[256];
+    for (int t = 0; t < nthreads; t++) {
+        entries_job_t j = {start_hashes, mixins, has_mixin, expected, num_hashes, ok, out_hashes,
+                           n * t / nthreads, n * (t + 1) / nthreads};
+        jobs[t] = j;
+    }
+    for (int t = 1; t < nthreads; t++) pthread_create(&th[t], NULL, entries_run, &jobs[t]);
+    entries_run(&jobs[0]);
+    for (int t = 1; t < nthreads; t++) pthread_join(th[t], NULL);
+}
+
+/* Recording: chain c starts from hashes[c] and runs entries
+ * first[c] .. first[c + 1] - 1 in order; entry e's hash goes to
+ * entry_hashes[e], and hashes[c] ends as the chain's last hash. */
+void oracle_poh_record(u8 *hashes, size_t chains, const u64 *first, const u64 *num_hashes, const u8 *mixins,
+                       const u8 *has_mixin, u8 *entry_hashes) {
+    for (size_t c = 0; c < chains; c++) {
+        u8 *h = hashes + 32 * c;
+        for (u64 e = first[c]; e < first[c + 1]; e++) {
+            oracle_poh_entry(h, num_hashes[e], has_mixin[e] ? mixins + 32 * e : NULL);
+            memcpy(entry_hashes + 32 * e, h, 32);
+        }
+    }
+}
+
 void oracle_create_keypairs(const u8 *seeds, u8 *pk, u8 *sk, size_t n, int nthreads) {
     job_t j = {0};
     j.kind = 3;

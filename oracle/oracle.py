@@ -87,6 +87,10 @@ class Oracle(_Lib):
         L.oracle_create_keypairs.argtypes = [_u8p, _u8p, _u8p, ctypes.c_size_t, ctypes.c_int]
         L.oracle_parse_packets.argtypes = [_u8p, ctypes.c_uint64, ctypes.c_uint32, _u32p] + [_u32p] * 5
         L.oracle_parse_packets.restype = None
+        L.oracle_poh_entry.argtypes = [_u8p, ctypes.c_uint64, _u8p]
+        L.oracle_poh_verify_entries.argtypes = [_u8p, _u64p, _u8p, _u8p, _u8p, ctypes.c_size_t, _u8p, _u8p,
+                                                ctypes.c_int]
+        L.oracle_poh_record.argtypes = [_u8p, ctypes.c_size_t, _u64p, _u64p, _u8p, _u8p, _u8p]
 
     # ---- single items -----------------------------------------------------
     def create_keypair(self, seed: bytes):
@@ -229,6 +233,40 @@ class Oracle(_Lib):
         bad = np.zeros(len(counts), dtype=np.int64)
         np.add.at(bad, pkt, (sig == 0).astype(np.int64))
         return ((counts > 0) & (bad == 0)).astype(np.uint8), sig, counts
+
+    # ---- PoH entries with transaction mixins (Solana ledger entries) ---------
+    def poh_entry(self, h: bytes, num_hashes: int, mixin: bytes | None) -> bytes:
+        buf = _bytes_arg(h)
+        self.lib.oracle_poh_entry(buf, num_hashes, _bytes_arg(mixin) if mixin is not None else None)
+        return bytes(buf)
+
+    def poh_verify_entries(self, start, num_hashes, mixins, has_mixin, expected, nthreads: int = 0):
+        """(ok per entry, computed entry hashes)."""
+        start = np.ascontiguousarray(start, dtype=np.uint8).reshape(-1, 32)
+        n = len(start)
+        nh = np.ascontiguousarray(num_hashes, dtype=np.uint64)
+        mx = np.ascontiguousarray(mixins, dtype=np.uint8).reshape(-1, 32)
+        hm = np.ascontiguousarray(has_mixin, dtype=np.uint8)
+        ex = np.ascontiguousarray(expected, dtype=np.uint8).reshape(-1, 32)
+        ok = np.zeros(n, dtype=np.uint8)
+        out = np.zeros((n, 32), dtype=np.uint8)
+        self.lib.oracle_poh_verify_entries(_ptr(start, _u8p), _ptr(nh, _u64p), _ptr(mx, _u8p), _ptr(hm, _u8p),
+                                           _ptr(ex, _u8p), n, _ptr(ok, _u8p), _ptr(out, _u8p),
+                                           nthreads or os.cpu_count() or 1)
+        return ok, out
+
+    def poh_record(self, start, first, num_hashes, mixins, has_mixin):
+        """(entry hashes, final hash per chain); chain c runs entries
+        first[c] .. first[c + 1] - 1."""
+        h = np.array(start, dtype=np.uint8, copy=True).reshape(-1, 32)
+        fi = np.ascontiguousarray(first, dtype=np.uint64)
+        nh = np.ascontiguousarray(num_hashes, dtype=np.uint64)
+        mx = np.ascontiguousarray(mixins, dtype=np.uint8).reshape(-1, 32)
+        hm = np.ascontiguousarray(has_mixin, dtype=np.uint8)
+        out = np.zeros((len(nh), 32), dtype=np.uint8)
+        self.lib.oracle_poh_record(_ptr(h, _u8p), len(h), _ptr(fi, _u64p), _ptr(nh, _u64p), _ptr(mx, _u8p),
+                                   _ptr(hm, _u8p), _ptr(out, _u8p))
+        return out, h
 
     def poh_verify_many(self, hashes: np.ndarray, num_hashes, nthreads: int = 1) -> np.ndarray:
         """Returns the final hashes (the input array is not modified)."""

@@ -151,7 +151,8 @@ bool init_locked() {
         if (ok)
             ok = preload_verify_kernels() == cudaSuccess && preload_sign_kernels() == cudaSuccess &&
                  preload_poh_kernels() == cudaSuccess && preload_poh_batch_kernels() == cudaSuccess &&
-                 preload_sig_batch_kernels() == cudaSuccess && preload_packets_kernels() == cudaSuccess;
+                 preload_sig_batch_kernels() == cudaSuccess && preload_packets_kernels() == cudaSuccess &&
+                 preload_sig_service_kernels() == cudaSuccess && preload_poh_entries_kernels() == cudaSuccess;
         if (!ok) {
             fprintf(stderr, "libcuda-crypt: GPU %d unusable: %s\n", d, cudaGetErrorString(cudaGetLastError()));
             break;
@@ -930,6 +931,137 @@ int gb300_poh_verify_batch(uint8_t* hashes, const uint64_t* num_hashes_arr, size
     cudaError_t e = run();
     if (e != cudaSuccess) {
         fprintf(stderr, "libcuda-crypt: gb300_poh_verify_batch failed: %s\n", cudaGetErrorString(e));
+        cudaGetLastError();
+    }
+    return t_last_error = (int)e;
+}
+
+// ---- Solana ledger entries (poh_entries.cu) ----
+
+size_t gb300_poh_entries_workspace_size(uint64_t num_entries) { return poh_entries_workspace_size(num_entries); }
+
+int gb300_poh_verify_entries_device(const uint8_t* start_hashes, const uint64_t* num_hashes, const uint8_t* mixins,
+                                    const uint8_t* has_mixin, const uint8_t* expected, uint64_t num_entries,
+                                    uint8_t* ok, uint8_t* out_hashes, void* workspace, size_t workspace_bytes,
+                                    void* stream) {
+    if (num_entries == 0) return 0;
+    if (!start_hashes || !num_hashes || !mixins || !has_mixin || !expected || !ok || !workspace ||
+        num_entries > 0xffffffffull)
+        return (int)cudaErrorInvalidValue;
+    if (workspace_bytes < poh_entries_workspace_size(num_entries)) return (int)cudaErrorInvalidValue;
+    if (((reinterpret_cast<uintptr_t>(start_hashes) | reinterpret_cast<uintptr_t>(mixins) |
+          reinterpret_cast<uintptr_t>(expected) | reinterpret_cast<uintptr_t>(out_hashes) |
+          reinterpret_cast<uintptr_t>(workspace)) & 15u) ||
+        (reinterpret_cast<uintptr_t>(num_hashes) & 7u))
+        return (int)cudaErrorMisalignedAddress;
+    Device* D = current_device();
+    if (!D) return (int)cudaErrorNoDevice;
+    const Tuning& T = tuning_for(*D);
+    return (int)launch_poh_verify_entries(start_hashes, num_hashes, mixins, has_mixin, expected, num_entries, ok,
+                                          out_hashes, workspace, 4 * D->sms * T.poh_warps_per_smsp,
+                                          static_cast<cudaStream_t>(stream));
+}
+
+int gb300_poh_verify_entries(const uint8_t* start_hashes, const uint64_t* num_hashes, const uint8_t* mixins,
+                             const uint8_t* has_mixin, const uint8_t* expected, size_t num_entries, uint8_t* ok) {
+    if (num_entries == 0) return 0;
+    if (!start_hashes || !num_hashes || !mixins || !has_mixin || !expected || !ok || num_entries > 0xffffffffull)
+        return t_last_error = (int)cudaErrorInvalidValue;
+    Lease L;
+    if (!acquire(L)) return 1;
+    const Tuning& T = tuning_for(*L.dev);
+    Queue& Q = *L.q;
+    cudaStream_t s = Q.stream;
+    const uint64_t n = num_entries;
+    // staging / device layout: start | expected | mixins | counts | flags
+    const size_t hb = 32 * n, cb = 8 * n, in_bytes = 3 * hb + cb + n;
+    auto run = [&]() -> cudaError_t {
+        TRY(Q.d_data.ensure(round_up(in_bytes, 256), s));
+        TRY(Q.d_scratch.ensure(poh_entries_workspace_size(n), s));
+        TRY(Q.d_out.ensure(n, s));
+        TRY(Q.h_stage.ensure(in_bytes));
+        uint8_t* st = static_cast<uint8_t*>(Q.h_stage.p);
+        memcpy(st, start_hashes, hb);
+        memcpy(st + hb, expected, hb);
+        memcpy(st + 2 * hb, mixins, hb);
+        memcpy(st + 3 * hb, num_hashes, cb);
+        memcpy(st + 3 * hb + cb, has_mixin, n);
+        uint8_t* d = static_cast<uint8_t*>(Q.d_data.p);
+        TRY(cudaMemcpyAsync(d, st, in_bytes, cudaMemcpyHostToDevice, s));
+        TRY(launch_poh_verify_entries(d, reinterpret_cast<const uint64_t*>(d + 3 * hb), d + 2 * hb, d + 3 * hb + cb,
+                                      d + hb, n, static_cast<uint8_t*>(Q.d_out.p), nullptr, Q.d_scratch.p,
+                                      4 * L.dev->sms * T.poh_warps_per_smsp, s));
+        TRY(cudaMemcpyAsync(st, Q.d_out.p, n, cudaMemcpyDeviceToHost, s));
+        TRY(cudaStreamSynchronize(s));
+        memcpy(ok, st, n);
+        return cudaSuccess;
+    };
+    cudaError_t e = run();
+    if (e != cudaSuccess) {
+        fprintf(stderr, "libcuda-crypt: gb300_poh_verify_entries failed: %s\n", cudaGetErrorString(e));
+        cudaGetLastError();
+    }
+    return t_last_error = (int)e;
+}
+
+int gb300_poh_record_device(uint8_t* hashes, uint64_t num_chains, const uint64_t* first, uint64_t num_entries,
+                            const uint64_t* num_hashes, const uint8_t* mixins, const uint8_t* has_mixin,
+                            uint8_t* entry_hashes, void* stream) {
+    if (num_chains == 0) return 0;
+    if (!hashes || !first || !num_hashes || !mixins || !has_mixin || !entry_hashes) return (int)cudaErrorInvalidValue;
+    if (((reinterpret_cast<uintptr_t>(hashes) | reinterpret_cast<uintptr_t>(mixins) |
+          reinterpret_cast<uintptr_t>(entry_hashes)) & 15u) ||
+        ((reinterpret_cast<uintptr_t>(first) | reinterpret_cast<uintptr_t>(num_hashes)) & 7u))
+        return (int)cudaErrorMisalignedAddress;
+    if (!current_device()) return (int)cudaErrorNoDevice;
+    return (int)launch_poh_record(hashes, num_chains, first, num_entries, num_hashes, mixins, has_mixin, entry_hashes,
+                                  static_cast<cudaStream_t>(stream));
+}
+
+int gb300_poh_record(uint8_t* hashes, size_t num_chains, const uint64_t* first, const uint64_t* num_hashes,
+                     const uint8_t* mixins, const uint8_t* has_mixin, uint8_t* entry_hashes) {
+    if (num_chains == 0) return 0;
+    if (!hashes || !first || !num_hashes || !mixins || !has_mixin || !entry_hashes)
+        return t_last_error = (int)cudaErrorInvalidValue;
+    // the chains' entry ranges must be well formed before anything is copied
+    if (first[0] != 0) return t_last_error = (int)cudaErrorInvalidValue;
+    for (size_t c = 0; c < num_chains; c++)
+        if (first[c + 1] < first[c]) return t_last_error = (int)cudaErrorInvalidValue;
+    const uint64_t ne = first[num_chains];
+    if (ne > 0xffffffffull) return t_last_error = (int)cudaErrorInvalidValue;
+    Lease L;
+    if (!acquire(L)) return 1;
+    Queue& Q = *L.q;
+    cudaStream_t s = Q.stream;
+    const uint64_t C = num_chains, E = ne ? ne : 1;
+    // staging / device layout: chain hashes | mixins | entry hashes (out) | first | counts | flags
+    const size_t hc = 32 * C, he = 32 * E, fb = 8 * (C + 1), cb = 8 * E;
+    const size_t total = hc + 2 * he + fb + cb + E;
+    auto run = [&]() -> cudaError_t {
+        TRY(Q.d_data.ensure(round_up(total, 256), s));
+        TRY(Q.h_stage.ensure(total));
+        uint8_t* st = static_cast<uint8_t*>(Q.h_stage.p);
+        memcpy(st, hashes, hc);
+        if (ne) {
+            memcpy(st + hc, mixins, 32 * ne);
+            memcpy(st + hc + 2 * he + fb, num_hashes, 8 * ne);
+            memcpy(st + hc + 2 * he + fb + cb, has_mixin, ne);
+        }
+        memcpy(st + hc + 2 * he, first, fb);
+        uint8_t* d = static_cast<uint8_t*>(Q.d_data.p);
+        TRY(cudaMemcpyAsync(d, st, total, cudaMemcpyHostToDevice, s));
+        TRY(launch_poh_record(d, C, reinterpret_cast<const uint64_t*>(d + hc + 2 * he), ne,
+                              reinterpret_cast<const uint64_t*>(d + hc + 2 * he + fb), d + hc,
+                              d + hc + 2 * he + fb + cb, d + hc + he, s));
+        TRY(cudaMemcpyAsync(st, d, hc + 2 * he, cudaMemcpyDeviceToHost, s));
+        TRY(cudaStreamSynchronize(s));
+        memcpy(hashes, st, hc);
+        if (ne) memcpy(entry_hashes, st + hc + he, 32 * ne);
+        return cudaSuccess;
+    };
+    cudaError_t e = run();
+    if (e != cudaSuccess) {
+        fprintf(stderr, "libcuda-crypt: gb300_poh_record failed: %s\n", cudaGetErrorString(e));
         cudaGetLastError();
     }
     return t_last_error = (int)e;

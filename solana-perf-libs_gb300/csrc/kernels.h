@@ -106,6 +106,75 @@ struct SigWork {
 };
 cudaError_t launch_sig_batch(const SigWork& w, int threads, int blocks_per_sm, int sms, cudaStream_t s);
 
+// Solana ledger entries (poh_entries.cu): PoH chains with transaction
+// mixins.  Verification runs every entry's plain hashes as one ragged PoH
+// batch, then the mixin step and the comparison; the workspace holds
+// poh_entries_workspace_size(n) bytes (256-byte aligned).  Recording runs
+// independent chains of entries, one thread per chain.
+size_t poh_entries_workspace_size(uint64_t n);
+cudaError_t launch_poh_verify_entries(const uint8_t* start, const uint64_t* num_hashes, const uint8_t* mixins,
+                                      const uint8_t* has_mixin, const uint8_t* expected, uint64_t n, uint8_t* ok,
+                                      uint8_t* out_hashes, void* ws, int warps, cudaStream_t s);
+cudaError_t launch_poh_record(uint8_t* hashes, uint64_t chains, const uint64_t* first, uint64_t num_entries,
+                              const uint64_t* num_hashes, const uint8_t* mixins, const uint8_t* has_mixin,
+                              uint8_t* entry_hashes, cudaStream_t s);
+cudaError_t preload_poh_entries_kernels();
+
+// Resident signature service (sig_service.cu) for the served loop: warps of
+// one long-lived launch take chunks of signature work from a FIFO in order
+// of publication and report each request's completion to the host as soon
+// as its last chunk is done.
+//   * requests and chunk descriptors live in page-locked host memory the GPU
+//     reads (written by the host before the chunks are published);
+//   * packets and the per-signature arrays are copied to device memory, and
+//     the chunks are published by a stream write of `tail` that follows
+//     those copies on the same stream (so a published chunk's inputs are in
+//     place);
+//   * results go straight into page-locked host memory, then the request's
+//     slot in `done` receives its generation number.
+struct alignas(16) SvcReq {
+    SigBatch b;              // n = the request's items; out: host memory the GPU writes
+    uint32_t gen;            // written to done[slot] when the last item is done
+    uint32_t pad[3];
+};
+enum SvcMode : uint32_t { kSvcVerify = 0, kSvcVerifyQuad = 1, kSvcSign = 2 };
+struct alignas(16) SvcChunk {
+    uint32_t req;            // request slot
+    uint32_t first;          // first item
+    uint32_t count;          // items: 1..32 (1..8 for kSvcVerifyQuad)
+    uint32_t mode;           // SvcMode
+};
+struct SvcDevice {           // device memory, zeroed at creation
+    uint32_t tail;           // chunks published
+    uint32_t head;           // chunks claimed
+    uint32_t stop;           // nonzero: warps leave as soon as the FIFO is empty
+    uint32_t exiting;        // nonzero: the launch is idle and every warp leaves (reset before a launch)
+    uint64_t last_claim_ns;  // %globaltimer of the launch's latest claim (reset before a launch)
+    uint32_t warps;          // warps that started (diagnostic)
+    uint32_t pad;
+};
+struct SvcParams {
+    SvcDevice* dev;
+    uint32_t* items_done;    // device memory [max_req], zeroed; each slot returns to 0 on completion
+    const SvcReq* req;       // device view of the host request table [max_req]
+    const SvcChunk* ring;    // device view of the host chunk ring [ring_size], ring_size a power of two
+    uint32_t* done;          // device view of the host completion words [max_req]
+    uint64_t* first_claim;   // device memory [max_req], all ones between requests: %globaltimer of a
+                             // request's first claimed chunk
+    uint64_t* times;         // device view of host memory [2 * max_req]: a completed request's first
+                             // claim and completion times (%globaltimer), written before `done`
+    uint32_t ring_size;
+    uint64_t idle_ns;        // the launch leaves (all warps together) after this long without a claim
+    const CurveTables* tables;
+};
+// Blocks of the service kernel that fit on one SM (sets its shared-memory
+// attributes on the current device first).
+cudaError_t sig_service_blocks_per_sm(int* blocks);
+cudaError_t launch_sig_service(const SvcParams& p, int blocks_per_sm, int sms, cudaStream_t s);
+// One thread writes %globaltimer to *out (device-visible memory).
+cudaError_t launch_svc_clock(uint64_t* out, cudaStream_t s);
+cudaError_t preload_sig_service_kernels();
+
 // Solana wire-format packet batches (packets.cu): `n` packet slots `stride`
 // bytes apart in one device buffer, lens[i] bytes of transaction data in
 // slot i.  The workspace (packets_workspace_size bytes, 256-byte aligned)

@@ -395,10 +395,29 @@ __global__ void __launch_bounds__(64 * P) poh_pair_persistent_kernel(uint8_t* ha
 
 }  // namespace
 
+// The persistent PoH kernels run for up to seconds beside signature work.
+// An SM's split between L1 and shared memory is set for the blocks it holds;
+// a block that needs more shared memory than that split gives cannot be
+// placed there until the SM drains.  With the driver's own split for these
+// kernels (14 KB of shared memory per pair block), the served loop's
+// resident signature kernel (60 KB per block) could wait behind running PoH
+// launches.  The chains live in registers and use no L1, so these kernels
+// ask for the largest shared-memory split, as the resident signature kernel
+// does.
 cudaError_t preload_poh_batch_kernels() {
-    return load_kernels(poh_hist_kernel, poh_scan_kernel, poh_scatter_kernel, poh_choose_kernel, poh_requeue_kernel,
-                        poh_persistent_kernel<1>, poh_persistent_kernel<4>, poh_pair_persistent_kernel<1>,
-                        poh_pair_persistent_kernel<2>);
+    cudaError_t e = load_kernels(poh_hist_kernel, poh_scan_kernel, poh_scatter_kernel, poh_choose_kernel,
+                                 poh_requeue_kernel, poh_persistent_kernel<1>, poh_persistent_kernel<4>,
+                                 poh_pair_persistent_kernel<1>, poh_pair_persistent_kernel<2>);
+    const int pref = cudaSharedmemCarveoutMaxShared;
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(poh_persistent_kernel<1>, cudaFuncAttributePreferredSharedMemoryCarveout, pref);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(poh_persistent_kernel<4>, cudaFuncAttributePreferredSharedMemoryCarveout, pref);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(poh_pair_persistent_kernel<1>, cudaFuncAttributePreferredSharedMemoryCarveout, pref);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(poh_pair_persistent_kernel<2>, cudaFuncAttributePreferredSharedMemoryCarveout, pref);
+    return e;
 }
 
 size_t poh_batch_workspace_size(uint64_t n) { return sizeof(PohBatchScratch) + 4ull * (n ? n : 1); }

@@ -19,10 +19,23 @@
 // and stay resident, as do the basepoint tables; merged launches are kept
 // within a slot's ring, so steady-state serving never allocates (a single
 // request larger than a ring grows it with the stream-ordered allocator).
+//
+// Verify/sign jobs (offset form) go by default to the resident signature
+// service instead (sig_service.cu): the submitting thread stages the job
+// into rings allocated at creation, copies its inputs to the GPU and
+// publishes its 32-item chunks to the FIFO of a long-lived kernel; the
+// dispatcher returns each request as soon as the GPU has written its
+// completion word, independently of what else is in flight, and launches
+// the kernel again whenever requests are waiting and it has left.  A job
+// too large for the rings takes the slot path.
+#include <cuda.h>            // driver types of the stream write (the driver library is not linked)
 #include <cuda_runtime.h>
+#include <sys/prctl.h>
 
 #include <chrono>
+#include <climits>
 #include <condition_variable>
+#include <cstddef>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -37,6 +50,7 @@
 #include "host_buffers.h"
 #include "host_copy.h"
 #include "kernels.h"
+#include "ring_alloc.h"
 #include "tables.cuh"
 
 namespace {
@@ -90,6 +104,68 @@ struct Slot {
     cudaError_t err = cudaSuccess;
 };
 
+// ---- resident signature service: host state --------------------------------
+
+constexpr uint32_t kSvcMaxReq = 4096;              // request slots in flight
+constexpr uint32_t kSvcRing = 1u << 18;            // chunk descriptors (4 MiB)
+constexpr uint64_t kSvcStageBytes = 256ull << 20;  // page-locked staging: index arrays, pageable packets
+constexpr uint64_t kSvcResultBytes = 64ull << 20;  // page-locked results the GPU writes
+constexpr uint64_t kSvcDevBytes = 1ull << 30;      // device input ring (at most the memory cap)
+
+typedef CUresult (*WriteValue32Fn)(CUstream, CUdeviceptr, cuuint32_t, unsigned int);
+
+struct SvcInflight {
+    uint64_t ticket;
+    int kind;                    // 0 verify, 1 sign
+    uint32_t slot, gen;
+    uint64_t n;
+    uint8_t* out;                // caller's output
+    uint64_t out_bytes;
+    const uint8_t* res;          // the results in the page-locked ring
+    uint64_t id_dev, id_stage, id_res, id_chunk;
+    uint64_t dev_bytes;
+    int64_t t_pub;
+};
+
+struct SvcDone {
+    uint64_t ticket, n;
+    int status;                  // 1 done, < 0 error
+    int64_t t_pub, t_done;
+    float wait_ms, run_ms;       // GPU: publication to first claimed chunk, first claim to completion
+};
+
+struct SigService {
+    bool on = false;
+    std::mutex mu;               // ring allocation and the order of copies and publications
+    cudaStream_t copy = nullptr, run = nullptr;
+    cudaEvent_t run_done = nullptr;
+    bool launched = false;
+    SvcDevice* d_state = nullptr;
+    uint32_t* d_items = nullptr;
+    uint64_t* d_first = nullptr;
+    uint8_t* d_in = nullptr;
+    gb300::RingAlloc dev_ring, stage_ring, res_ring, chunks;
+    uint8_t* h_stage = nullptr;
+    uint8_t* h_res = nullptr;
+    uint8_t* d_res = nullptr;
+    void* h_ctl = nullptr;       // mapped: request table, chunk ring, completion words, times
+    SvcReq* h_req = nullptr;
+    SvcChunk* h_ring = nullptr;
+    uint32_t* h_done = nullptr;
+    uint64_t* h_times = nullptr; // [2 * kSvcMaxReq]: first claim, completion (%globaltimer)
+    int64_t clock_offset = 0;    // host steady-clock ns minus %globaltimer ns
+    SvcParams params{};
+    uint64_t chunk_tail = 0;     // chunks published (virtual count; the GPU sees the low 32 bits)
+    std::vector<uint32_t> free_slots, gen;
+    std::vector<SvcInflight> inflight;
+    std::deque<Req> pending;     // admitted in arrival order as ring space frees up
+    uint64_t in_use = 0;         // device bytes of the requests in flight
+    WriteValue32Fn write_value = nullptr;
+    int blocks_per_sm = 2;
+    uint64_t launches = 0, max_inflight = 0, served = 0, fallback = 0;
+    cudaError_t err = cudaSuccess;
+};
+
 }  // namespace
 
 struct gb300_server {
@@ -119,6 +195,7 @@ struct gb300_server {
         float copy_in_ms, kernels_ms, copy_out_ms;   // GPU time of each phase (events)
     };
     std::vector<Trace> trace;
+    SigService svc;
 };
 
 namespace {
@@ -343,10 +420,336 @@ void deliver(Slot& S) {
     }
 }
 
+// ---- resident signature service: host side --------------------------------
+
+// Publishes chunks [0, tail) to the service kernel: a stream write ordered
+// after the inputs' copies on the same stream (preceded by a system-wide
+// fence).  Without the driver entry point, a one-thread kernel does the same.
+__global__ void svc_publish_kernel(uint32_t* tail, uint32_t v) {
+    __threadfence_system();
+    *reinterpret_cast<volatile uint32_t*>(tail) = v;
+}
+
+cudaError_t svc_publish(SigService& V, uint32_t tail) {
+    if (V.write_value) {
+        const CUresult r = V.write_value(reinterpret_cast<CUstream>(V.copy),
+                                         reinterpret_cast<CUdeviceptr>(&V.d_state->tail), tail, 0);
+        if (r == CUDA_SUCCESS) return cudaSuccess;
+        V.write_value = nullptr;                 // not supported here: the kernel from now on
+    }
+    svc_publish_kernel<<<1, 1, 0, V.copy>>>(&V.d_state->tail, tail);
+    return cudaGetLastError();
+}
+
+uint64_t env_mib(const char* name, uint64_t dflt) {
+    const char* v = getenv(name);
+    return v && atoi(v) > 0 ? (uint64_t)atoi(v) << 20 : dflt;
+}
+
+bool svc_create(gb300_server* sv) {
+    SigService& V = sv->svc;
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    const uint64_t dev_bytes = std::min<uint64_t>(env_mib("GB300_CRYPT_SERVER_SVC_DEVICE_MB", kSvcDevBytes),
+                                                  round_up(sv->cap, 1ull << 20));
+    const uint64_t stage_bytes = env_mib("GB300_CRYPT_SERVER_SVC_STAGE_MB", kSvcStageBytes);
+    const uint64_t result_bytes = env_mib("GB300_CRYPT_SERVER_SVC_RESULT_MB", kSvcResultBytes);
+    const size_t ctl = sizeof(SvcReq) * kSvcMaxReq + sizeof(SvcChunk) * kSvcRing + 4ull * kSvcMaxReq +
+                       16ull * kSvcMaxReq;
+    bool ok = cudaStreamCreateWithPriority(&V.copy, cudaStreamNonBlocking, hi) == cudaSuccess &&
+              cudaStreamCreateWithPriority(&V.run, cudaStreamNonBlocking, hi) == cudaSuccess &&
+              cudaEventCreateWithFlags(&V.run_done, cudaEventDisableTiming) == cudaSuccess &&
+              cudaMalloc(&V.d_state, sizeof(SvcDevice)) == cudaSuccess &&
+              cudaMalloc(&V.d_items, 4ull * kSvcMaxReq) == cudaSuccess &&
+              cudaMalloc(&V.d_first, 8ull * kSvcMaxReq) == cudaSuccess &&
+              cudaMalloc(&V.d_in, dev_bytes) == cudaSuccess &&
+              cudaHostAlloc(&V.h_stage, stage_bytes, cudaHostAllocDefault) == cudaSuccess &&
+              cudaHostAlloc(&V.h_res, result_bytes, cudaHostAllocMapped) == cudaSuccess &&
+              cudaHostAlloc(&V.h_ctl, ctl, cudaHostAllocMapped) == cudaSuccess;
+    void *d_res = nullptr, *d_ctl = nullptr;
+    ok = ok && cudaHostGetDevicePointer(&d_res, V.h_res, 0) == cudaSuccess &&
+         cudaHostGetDevicePointer(&d_ctl, V.h_ctl, 0) == cudaSuccess;
+    ok = ok && cudaMemsetAsync(V.d_state, 0, sizeof(SvcDevice), V.copy) == cudaSuccess &&
+         cudaMemsetAsync(V.d_items, 0, 4ull * kSvcMaxReq, V.copy) == cudaSuccess &&
+         cudaMemsetAsync(V.d_first, 0xff, 8ull * kSvcMaxReq, V.copy) == cudaSuccess &&
+         cudaStreamSynchronize(V.copy) == cudaSuccess;
+    if (!ok) return false;
+    memset(V.h_ctl, 0, ctl);
+    V.d_res = static_cast<uint8_t*>(d_res);
+    V.h_req = static_cast<SvcReq*>(V.h_ctl);
+    V.h_ring = reinterpret_cast<SvcChunk*>(V.h_req + kSvcMaxReq);
+    V.h_done = reinterpret_cast<uint32_t*>(V.h_ring + kSvcRing);
+    V.h_times = reinterpret_cast<uint64_t*>(V.h_done + kSvcMaxReq);
+    auto* dreq = static_cast<SvcReq*>(d_ctl);
+    auto* dring = reinterpret_cast<SvcChunk*>(dreq + kSvcMaxReq);
+    V.dev_ring.reset(dev_bytes);
+    V.stage_ring.reset(stage_bytes);
+    V.res_ring.reset(result_bytes);
+    V.chunks.reset(kSvcRing, false);
+    V.free_slots.resize(kSvcMaxReq);
+    for (uint32_t k = 0; k < kSvcMaxReq; k++) V.free_slots[k] = kSvcMaxReq - 1 - k;
+    V.gen.assign(kSvcMaxReq, 0);
+    V.params.dev = V.d_state;
+    V.params.items_done = V.d_items;
+    V.params.req = dreq;
+    V.params.ring = dring;
+    V.params.done = reinterpret_cast<uint32_t*>(dring + kSvcRing);
+    V.params.first_claim = V.d_first;
+    V.params.times = reinterpret_cast<uint64_t*>(V.params.done + kSvcMaxReq);
+    V.params.ring_size = kSvcRing;
+    const char* idle = getenv("GB300_CRYPT_SERVER_IDLE_US");
+    V.params.idle_ns = 1000ull * (uint64_t)(idle && atoi(idle) > 0 ? atoi(idle) : 20000);
+    V.params.tables = sv->info.tables;
+    if (const char* b = getenv("GB300_CRYPT_SERVER_SVC_BLOCKS")) V.blocks_per_sm = atoi(b) > 0 ? atoi(b) : 2;
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuStreamWriteValue32", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+        V.write_value = reinterpret_cast<WriteValue32Fn>(fn);
+    cudaGetLastError();
+    if (load_kernels(svc_publish_kernel) != cudaSuccess) return false;
+    // the GPU clock against the host's: the best of a few round trips
+    {
+        int64_t best = INT64_MAX;
+        for (int k = 0; k < 5; k++) {
+            const int64_t t0 = now_ns();
+            if (launch_svc_clock(V.params.times, V.copy) != cudaSuccess ||
+                cudaStreamSynchronize(V.copy) != cudaSuccess)
+                return false;
+            const int64_t t1 = now_ns();
+            if (t1 - t0 < best) {
+                best = t1 - t0;
+                V.clock_offset = (t0 + t1) / 2 - (int64_t)__atomic_load_n(&V.h_times[0], __ATOMIC_ACQUIRE);
+            }
+        }
+        V.h_times[0] = 0;
+    }
+    V.on = true;
+    return true;
+}
+
+void svc_destroy(gb300_server* sv) {
+    SigService& V = sv->svc;
+    if (V.copy && V.d_state) {
+        // warps leave as soon as the FIFO is empty (everything published is done by now)
+        const uint32_t one = 1;
+        cudaMemcpyAsync(&V.d_state->stop, &one, 4, cudaMemcpyHostToDevice, V.copy);
+        cudaStreamSynchronize(V.copy);
+    }
+    if (V.run) cudaStreamSynchronize(V.run);
+    if (V.copy) cudaStreamSynchronize(V.copy);
+    if (V.d_state) cudaFree(V.d_state);
+    if (V.d_items) cudaFree(V.d_items);
+    if (V.d_first) cudaFree(V.d_first);
+    if (V.d_in) cudaFree(V.d_in);
+    if (V.h_stage) cudaFreeHost(V.h_stage);
+    if (V.h_res) cudaFreeHost(V.h_res);
+    if (V.h_ctl) cudaFreeHost(V.h_ctl);
+    if (V.run_done) cudaEventDestroy(V.run_done);
+    if (V.run) cudaStreamDestroy(V.run);
+    if (V.copy) cudaStreamDestroy(V.copy);
+    cudaGetLastError();
+    V.on = false;
+}
+
+// The kernel is running, or launched now when it has left and requests are
+// waiting on it (V.mu held).
+void svc_ensure_running(gb300_server* sv) {
+    SigService& V = sv->svc;
+    if (V.inflight.empty() || V.err != cudaSuccess) return;
+    if (V.launched) {
+        const cudaError_t q = cudaEventQuery(V.run_done);
+        if (q == cudaErrorNotReady) return;
+        if (q != cudaSuccess) {
+            V.err = q;
+            return;
+        }
+    }
+    // the launch's exit flag and claim time start from zero (stream order:
+    // after the previous launch has left)
+    cudaError_t e = cudaMemsetAsync(&V.d_state->exiting, 0, offsetof(SvcDevice, warps) - offsetof(SvcDevice, exiting),
+                                    V.run);
+    if (e == cudaSuccess) e = launch_sig_service(V.params, V.blocks_per_sm, sv->info.sms, V.run);
+    if (e == cudaSuccess) e = cudaEventRecord(V.run_done, V.run);
+    if (e != cudaSuccess) {
+        V.err = e;
+        return;
+    }
+    V.launched = true;
+    V.launches++;
+}
+
+// Stages and publishes one verify/sign job (V.mu held).  1: published; 0: the
+// rings have no room now (retry after completions); -1: it never fits the
+// rings (take the slot path).
+int svc_try_submit(gb300_server* sv, const Req& r) {
+    SigService& V = sv->svc;
+    const gb300_sig_job& J = r.job;
+    const uint64_t n = r.n;
+    const bool verify = r.kind == 0;
+    // four lanes per signature while the verifies in flight leave the GPU
+    // idle (the size rule of the one-call form: up to 64 per SM)
+    uint64_t v_inflight = 0;
+    for (const SvcInflight& f : V.inflight)
+        if (f.kind == 0) v_inflight += f.n;
+    const bool quad = verify && v_inflight + n <= 64ull * (uint64_t)sv->info.sms;
+    const uint32_t per = quad ? 8u : 32u;
+    const uint64_t nchunks = (n + per - 1) / per;
+    const uint64_t idx_bytes = 16 * n, pk_off = round_up(idx_bytes, 256);
+    const uint64_t dev_need = pk_off + J.packets_len + 16;
+    const uint64_t stage_need = pk_off + (r.locked ? 0 : J.packets_len);
+    const uint64_t res_need = verify ? n : 64 * n;
+    if (dev_need > V.dev_ring.capacity() || stage_need > V.stage_ring.capacity() ||
+        res_need > V.res_ring.capacity() || nchunks > V.chunks.capacity())
+        return -1;
+    if (V.free_slots.empty()) return 0;
+    if (V.in_use + r.bytes > sv->cap && !V.inflight.empty()) return 0;   // wait for memory
+    uint64_t dv, di, sp, si, rv, ri, cv, ci;
+    if (!V.dev_ring.alloc(dev_need, 256, &dv, &di)) return 0;
+    if (!V.stage_ring.alloc(stage_need, 256, &sp, &si)) {
+        V.dev_ring.release(di);
+        return 0;
+    }
+    if (!V.res_ring.alloc(res_need, 64, &rv, &ri)) {
+        V.dev_ring.release(di);
+        V.stage_ring.release(si);
+        return 0;
+    }
+    if (!V.chunks.alloc(nchunks, 1, &cv, &ci)) {
+        V.dev_ring.release(di);
+        V.stage_ring.release(si);
+        V.res_ring.release(ri);
+        return 0;
+    }
+    const uint32_t slot = V.free_slots.back();
+    V.free_slots.pop_back();
+    uint32_t gen = V.gen[slot] + 1;
+    if (gen == 0) gen = 1;
+    V.gen[slot] = gen;
+    uint8_t* stage = V.h_stage + sp % V.stage_ring.capacity();
+    uint8_t* din = V.d_in + dv % V.dev_ring.capacity();
+    uint8_t* res = V.h_res + rv % V.res_ring.capacity();
+    // the job's own arrays, verbatim: each item's offsets are checked on the
+    // GPU against the job's packet bytes
+    uint32_t* hidx = reinterpret_cast<uint32_t*>(stage);
+    memcpy(hidx, J.message_lens, 4 * n);
+    memcpy(hidx + n, J.public_key_offsets, 4 * n);
+    memcpy(hidx + 2 * n, J.key_offsets, 4 * n);
+    memcpy(hidx + 3 * n, J.message_start_offsets, 4 * n);
+    cudaError_t e = cudaSuccess;
+    if (!r.locked && J.packets_len) {
+        gb300::CopyPiece pc{stage + pk_off, J.packets, J.packets_len};
+        gb300::CopyPool::copy(&pc, 1);
+        e = cudaMemcpyAsync(din, stage, pk_off + J.packets_len, cudaMemcpyHostToDevice, V.copy);
+    } else {
+        e = cudaMemcpyAsync(din, stage, idx_bytes, cudaMemcpyHostToDevice, V.copy);
+        if (e == cudaSuccess && J.packets_len)
+            e = cudaMemcpyAsync(din + pk_off, J.packets, J.packets_len, cudaMemcpyHostToDevice, V.copy);
+    }
+    SvcReq& q = V.h_req[slot];
+    const uint32_t* di32 = reinterpret_cast<const uint32_t*>(din);
+    q.b = SigBatch{din + pk_off, J.packets_len, di32, di32 + n, di32 + 2 * n, di32 + 3 * n, (uint32_t)n,
+                   V.d_res + rv % V.res_ring.capacity(), sv->info.tables};
+    q.b.window = sv->info.verify_window;
+    q.gen = gen;
+    const uint32_t mode = verify ? (quad ? kSvcVerifyQuad : kSvcVerify) : kSvcSign;
+    for (uint64_t k = 0; k < nchunks; k++) {
+        SvcChunk& c = V.h_ring[(cv + k) % kSvcRing];
+        c.req = slot;
+        c.first = (uint32_t)(k * per);
+        c.count = (uint32_t)std::min<uint64_t>(per, n - k * per);
+        c.mode = mode;
+    }
+    V.chunk_tail = cv + nchunks;
+    if (e == cudaSuccess) e = svc_publish(V, (uint32_t)V.chunk_tail);
+    if (e != cudaSuccess) V.err = e;
+    V.inflight.push_back({r.ticket, r.kind, slot, gen, n, J.out, res_need, res, di, si, ri, ci, r.bytes, now_ns()});
+    V.in_use += r.bytes;
+    V.max_inflight = std::max<uint64_t>(V.max_inflight, V.inflight.size());
+    svc_ensure_running(sv);
+    return 1;
+}
+
+// Completed requests out of the FIFO (results to the callers, ring space
+// back), then queued requests in, then the kernel kept running (V.mu held).
+void svc_progress(gb300_server* sv, std::vector<SvcDone>& done, std::vector<Req>& to_slots) {
+    SigService& V = sv->svc;
+    for (size_t k = 0; k < V.inflight.size();) {
+        SvcInflight& f = V.inflight[k];
+        const bool ok = __atomic_load_n(&V.h_done[f.slot], __ATOMIC_ACQUIRE) == f.gen;
+        if (!ok && V.err == cudaSuccess) {
+            k++;
+            continue;
+        }
+        if (ok) memcpy(f.out, f.res, f.out_bytes);
+        else memset(f.out, 0, f.out_bytes);
+        float wait_ms = -1.f, run_ms = -1.f;
+        if (ok) {
+            const int64_t first = (int64_t)V.h_times[2 * f.slot] + V.clock_offset;
+            const int64_t end = (int64_t)V.h_times[2 * f.slot + 1] + V.clock_offset;
+            wait_ms = (float)((first - f.t_pub) * 1e-6);
+            run_ms = (float)((end - first) * 1e-6);
+        }
+        done.push_back({f.ticket, f.n, ok ? 1 : -(int)V.err, f.t_pub, now_ns(), wait_ms, run_ms});
+        V.dev_ring.release(f.id_dev);
+        V.stage_ring.release(f.id_stage);
+        V.res_ring.release(f.id_res);
+        V.chunks.release(f.id_chunk);
+        V.free_slots.push_back(f.slot);
+        V.in_use -= f.dev_bytes;
+        V.served++;
+        f = V.inflight.back();
+        V.inflight.pop_back();
+    }
+    while (!V.pending.empty()) {
+        const int rc = svc_try_submit(sv, V.pending.front());
+        if (rc == 0) break;
+        if (rc < 0) {
+            to_slots.push_back(V.pending.front());
+            V.fallback++;
+        }
+        V.pending.pop_front();
+    }
+    svc_ensure_running(sv);
+}
+
 void dispatcher(gb300_server* sv) {
     cudaSetDevice(sv->dev);
+    // the short waits below (a few us while the GPU has requests) would
+    // otherwise overshoot by the default 50 us timer slack
+    prctl(PR_SET_TIMERSLACK, 1000UL, 0, 0, 0);
     std::unique_lock<std::mutex> lk(sv->mu);
+    std::vector<SvcDone> svc_done;
+    std::vector<Req> to_slots;
     for (;;) {
+        // ---- resident signature service: completions, queued requests ----
+        bool svc_busy = false;
+        if (sv->svc.on) {
+            lk.unlock();
+            {
+                std::lock_guard<std::mutex> vl(sv->svc.mu);
+                svc_progress(sv, svc_done, to_slots);
+                svc_busy = !sv->svc.inflight.empty() || !sv->svc.pending.empty();
+            }
+            lk.lock();
+            for (const SvcDone& d : svc_done) {
+                auto it = sv->times.find(d.ticket);
+                if (it != sv->times.end()) {
+                    it->second.second = d.t_done;
+                    if (sv->trace.size() >= 4096) sv->trace.erase(sv->trace.begin(), sv->trace.begin() + 1024);
+                    sv->trace.push_back({4, 1u, d.n, it->second.first, d.t_pub, d.t_done, d.wait_ms, d.run_ms,
+                                         (float)((d.t_done - d.t_pub) * 1e-6)});
+                }
+                sv->status[d.ticket] = d.status;
+                sv->requests_done++;
+                sv->items_done += d.n;
+            }
+            if (!svc_done.empty()) sv->cv_done.notify_all();
+            svc_done.clear();
+            for (Req& r : to_slots) sv->pending_sig.push_back(r);
+            to_slots.clear();
+            if (sv->svc.max_inflight > sv->merged_max) sv->merged_max = sv->svc.max_inflight;
+        }
         // ---- completions ----
         bool any_busy = false;
         for (auto* slots : {&sv->sig_slots, &sv->poh_slots}) {
@@ -461,8 +864,10 @@ void dispatcher(gb300_server* sv) {
         bool busy = false;
         for (auto* slots : {&sv->sig_slots, &sv->poh_slots})
             for (auto& S : *slots) busy |= S.busy;
-        if (sv->stop && !busy && sv->pending_sig.empty() && sv->pending_poh.empty()) break;
-        if (busy || any_busy)
+        if (sv->stop && !busy && !svc_busy && sv->pending_sig.empty() && sv->pending_poh.empty()) break;
+        if (svc_busy)
+            sv->cv_work.wait_for(lk, std::chrono::microseconds(5));
+        else if (busy || any_busy)
             sv->cv_work.wait_for(lk, std::chrono::microseconds(20));
         else
             sv->cv_work.wait(lk);
@@ -504,7 +909,10 @@ gb300_server* gb300_server_create(const gb300_server_config* cfg) {
     }
     sv->cap = cfg && cfg->device_memory_cap ? cfg->device_memory_cap : (8ull << 30);
     sv->max_items = cfg && cfg->max_items_per_launch ? cfg->max_items_per_launch : 65536u;
-    const uint32_t nsig = cfg && cfg->sig_slots ? cfg->sig_slots : 3u;
+    const bool service = !cfg || cfg->sig_mode == 0;
+    // with the service, slots carry only wire-packet batches and jobs too
+    // large for the service's rings
+    const uint32_t nsig = cfg && cfg->sig_slots ? cfg->sig_slots : (service ? 2u : 3u);
     const uint32_t npoh = cfg && cfg->poh_slots ? cfg->poh_slots : 2u;
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);   // hi is the numerically smaller, higher priority
@@ -537,6 +945,7 @@ gb300_server* gb300_server_create(const gb300_server_config* cfg) {
     }
     for (auto* slots : {&sv->sig_slots, &sv->poh_slots})
         for (auto& S : *slots) ok = ok && cudaStreamSynchronize(S.stream) == cudaSuccess;
+    if (ok && service) ok = svc_create(sv);
     if (!ok) {
         gb300_server_destroy(sv);
         return nullptr;
@@ -556,6 +965,7 @@ void gb300_server_destroy(gb300_server* sv) {
     int prev = -1;
     cudaGetDevice(&prev);
     cudaSetDevice(sv->dev);
+    svc_destroy(sv);
     for (auto* slots : {&sv->sig_slots, &sv->poh_slots})
         for (auto& S : *slots) {
             if (S.stream) cudaStreamSynchronize(S.stream);
@@ -586,10 +996,27 @@ uint64_t gb300_server_submit_sigs(gb300_server* sv, const gb300_sig_job* job) {
     r.locked = !job->packets_len || page_locked(job->packets);
     r.bytes = sig_bytes(*job);
     if (r.bytes > sv->cap) return 0;   // a request above max_items runs in a launch of its own
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        r.ticket = sv->next_ticket++;
+        sv->status[r.ticket] = 0;
+        sv->times[r.ticket] = {now_ns(), -1};
+    }
+    if (sv->svc.on) {
+        // staged and published from this thread, in arrival order
+        int rc = 0;
+        {
+            std::lock_guard<std::mutex> vl(sv->svc.mu);
+            rc = sv->svc.pending.empty() ? svc_try_submit(sv, r) : 0;
+            if (rc == 0) sv->svc.pending.push_back(r);
+            if (rc < 0) sv->svc.fallback++;
+        }
+        if (rc >= 0) {
+            sv->cv_work.notify_one();
+            return r.ticket;
+        }
+    }
     std::lock_guard<std::mutex> lk(sv->mu);
-    r.ticket = sv->next_ticket++;
-    sv->status[r.ticket] = 0;
-    sv->times[r.ticket] = {now_ns(), -1};
     sv->pending_sig.push_back(r);
     sv->cv_work.notify_one();
     return r.ticket;
@@ -712,14 +1139,28 @@ int gb300_server_trace(gb300_server* sv, char* buf, size_t len) {
 int gb300_server_stats(gb300_server* sv, char* buf, size_t len) {
     if (!sv || !buf || len == 0) return 0;
     std::lock_guard<std::mutex> lk(sv->mu);
+    uint64_t sl = 0, sm = 0, ss = 0, sf = 0, sp = 0, si = 0;
+    {
+        std::lock_guard<std::mutex> vl(sv->svc.mu);
+        sl = sv->svc.launches;
+        sm = sv->svc.max_inflight;
+        ss = sv->svc.served;
+        sf = sv->svc.fallback;
+        sp = sv->svc.pending.size();
+        si = sv->svc.in_use;
+    }
     int n = snprintf(buf, len,
                      "{\"device\": %d, \"launches_sig\": %llu, \"launches_poh\": %llu, \"requests_done\": %llu, "
                      "\"items_done\": %llu, \"max_requests_merged\": %llu, \"pending_sig\": %zu, "
-                     "\"pending_poh\": %zu, \"device_bytes_in_flight\": %llu, \"device_memory_cap\": %llu}",
-                     sv->dev, (unsigned long long)sv->launches_sig, (unsigned long long)sv->launches_poh,
+                     "\"pending_poh\": %zu, \"device_bytes_in_flight\": %llu, \"device_memory_cap\": %llu, "
+                     "\"service\": {\"on\": %d, \"launches\": %llu, \"max_in_flight\": %llu, \"served\": %llu, "
+                     "\"to_slots\": %llu, \"pending\": %llu, \"device_bytes_in_flight\": %llu}}",
+                     sv->dev, (unsigned long long)(sv->launches_sig + sl), (unsigned long long)sv->launches_poh,
                      (unsigned long long)sv->requests_done, (unsigned long long)sv->items_done,
                      (unsigned long long)sv->merged_max, sv->pending_sig.size(), sv->pending_poh.size(),
-                     (unsigned long long)sv->in_use, (unsigned long long)sv->cap);
+                     (unsigned long long)sv->in_use, (unsigned long long)sv->cap, sv->svc.on ? 1 : 0,
+                     (unsigned long long)sl, (unsigned long long)sm, (unsigned long long)ss, (unsigned long long)sf,
+                     (unsigned long long)sp, (unsigned long long)si);
     return n < 0 ? 0 : (n < (int)len ? n : (int)len - 1);
 }
 

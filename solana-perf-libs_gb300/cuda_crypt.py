@@ -289,6 +289,80 @@ class CudaCrypt:
         if rc != 0:
             raise RuntimeError(f"gb300_poh_verify_batch_shape: cudaError {rc}")
 
+    # ---- Solana ledger entries: PoH chains with transaction mixins ----
+    def _entries_types(self):
+        L = self.lib
+        if getattr(self, "_entries_ready", False):
+            return L
+        L.gb300_poh_entries_workspace_size.argtypes = [ctypes.c_uint64]
+        L.gb300_poh_entries_workspace_size.restype = ctypes.c_size_t
+        L.gb300_poh_verify_entries.argtypes = [_u8p, _u64p, _u8p, _u8p, _u8p, ctypes.c_size_t, _u8p]
+        L.gb300_poh_verify_entries.restype = ctypes.c_int
+        L.gb300_poh_verify_entries_device.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_uint64] + \
+            [ctypes.c_void_p] * 3 + [ctypes.c_size_t, ctypes.c_void_p]
+        L.gb300_poh_verify_entries_device.restype = ctypes.c_int
+        L.gb300_poh_record.argtypes = [_u8p, ctypes.c_size_t, _u64p, _u64p, _u8p, _u8p, _u8p]
+        L.gb300_poh_record.restype = ctypes.c_int
+        L.gb300_poh_record_device.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64] + \
+            [ctypes.c_void_p] * 5
+        L.gb300_poh_record_device.restype = ctypes.c_int
+        self._entries_ready = True
+        return L
+
+    def poh_entries_workspace_size(self, n: int) -> int:
+        return int(self._entries_types().gb300_poh_entries_workspace_size(n))
+
+    def poh_verify_entries(self, start, num_hashes, mixins, has_mixin, expected) -> np.ndarray:
+        """ok per entry (host form); 32-byte arrays as (n, 32) uint8."""
+        L = self._entries_types()
+        st = np.ascontiguousarray(start, dtype=np.uint8).reshape(-1, 32)
+        n = len(st)
+        nh = np.ascontiguousarray(num_hashes, dtype=np.uint64)
+        mx = np.ascontiguousarray(mixins, dtype=np.uint8).reshape(-1, 32)
+        hm = np.ascontiguousarray(has_mixin, dtype=np.uint8)
+        ex = np.ascontiguousarray(expected, dtype=np.uint8).reshape(-1, 32)
+        ok = np.zeros(n, dtype=np.uint8)
+        rc = L.gb300_poh_verify_entries(_p(st, _u8p), _p(nh, _u64p), _p(mx, _u8p), _p(hm, _u8p), _p(ex, _u8p), n,
+                                        _p(ok, _u8p))
+        if rc != 0:
+            raise RuntimeError(f"gb300_poh_verify_entries: cudaError {rc}")
+        return ok
+
+    def poh_verify_entries_device(self, start, num_hashes, mixins, has_mixin, expected, ok, out_hashes, workspace,
+                                  stream=0) -> None:
+        L = self._entries_types()
+        rc = L.gb300_poh_verify_entries_device(start.data_ptr(), num_hashes.data_ptr(), mixins.data_ptr(),
+                                               has_mixin.data_ptr(), expected.data_ptr(), num_hashes.numel(),
+                                               ok.data_ptr(), out_hashes.data_ptr() if out_hashes is not None else None,
+                                               workspace.data_ptr(), workspace.numel() * workspace.element_size(),
+                                               stream)
+        if rc != 0:
+            raise RuntimeError(f"gb300_poh_verify_entries_device: cudaError {rc}")
+
+    def poh_record(self, start, first, num_hashes, mixins, has_mixin):
+        """(entry hashes, last hash per chain) (host form); chain c runs
+        entries first[c] .. first[c + 1] - 1."""
+        L = self._entries_types()
+        h = np.array(start, dtype=np.uint8, copy=True).reshape(-1, 32)
+        fi = np.ascontiguousarray(first, dtype=np.uint64)
+        nh = np.ascontiguousarray(num_hashes, dtype=np.uint64)
+        mx = np.ascontiguousarray(mixins, dtype=np.uint8).reshape(-1, 32)
+        hm = np.ascontiguousarray(has_mixin, dtype=np.uint8)
+        out = np.zeros((max(1, len(nh)), 32), dtype=np.uint8)
+        rc = L.gb300_poh_record(_p(h, _u8p), len(h), _p(fi, _u64p), _p(nh, _u64p), _p(mx, _u8p), _p(hm, _u8p),
+                                _p(out, _u8p))
+        if rc != 0:
+            raise RuntimeError(f"gb300_poh_record: cudaError {rc}")
+        return out[:len(nh)], h
+
+    def poh_record_device(self, hashes, first, num_hashes, mixins, has_mixin, entry_hashes, stream=0) -> None:
+        L = self._entries_types()
+        rc = L.gb300_poh_record_device(hashes.data_ptr(), first.numel() - 1, first.data_ptr(), num_hashes.numel(),
+                                       num_hashes.data_ptr(), mixins.data_ptr(), has_mixin.data_ptr(),
+                                       entry_hashes.data_ptr(), stream)
+        if rc != 0:
+            raise RuntimeError(f"gb300_poh_record_device: cudaError {rc}")
+
     # ---- Solana wire-format packets (gb300_packets.h) ----
     def packets_workspace_size(self, n: int, stride: int) -> int:
         return int(self.lib.gb300_packets_workspace_size(n, stride))
@@ -397,14 +471,17 @@ class CudaCrypt:
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("device_memory_cap", ctypes.c_uint64), ("sig_slots", ctypes.c_uint32),
-                ("poh_slots", ctypes.c_uint32), ("max_items_per_launch", ctypes.c_uint32)]
+                ("poh_slots", ctypes.c_uint32), ("max_items_per_launch", ctypes.c_uint32),
+                ("sig_mode", ctypes.c_uint32)]
+
+SIG_SERVICE, SIG_SLOTS = 0, 1       # ServerConfig.sig_mode
 
 
 class Server:
     """The served request loop (include/gb300_serve.h) on the current GPU."""
 
     def __init__(self, lib: "CudaCrypt", device_memory_cap: int = 0, sig_slots: int = 0, poh_slots: int = 0,
-                 max_items_per_launch: int = 0):
+                 max_items_per_launch: int = 0, sig_mode: int = SIG_SERVICE):
         L = self.L = lib.lib
         L.gb300_server_create.argtypes = [ctypes.POINTER(ServerConfig)]
         L.gb300_server_create.restype = ctypes.c_void_p
@@ -424,7 +501,7 @@ class Server:
         L.gb300_server_submit_packets.restype = ctypes.c_uint64
         L.gb300_server_trace.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]
         L.gb300_server_trace.restype = ctypes.c_int
-        cfg = ServerConfig(device_memory_cap, sig_slots, poh_slots, max_items_per_launch)
+        cfg = ServerConfig(device_memory_cap, sig_slots, poh_slots, max_items_per_launch, sig_mode)
         self.h = L.gb300_server_create(ctypes.byref(cfg))
         if not self.h:
             raise RuntimeError("gb300_server_create failed")

@@ -19,6 +19,8 @@ Workloads (sizes and distributions of the reference-facing benchmark set):
                    message bit.
   poh_ragged       16384 entries, num_hashes log-uniform in 1..1e6, 3%
                    corrupted expected hashes.
+  poh_entries      chains of Solana ledger entries: ticks (12500 hashes) and
+                   transaction entries (1..64 hashes and a 32-byte mixin).
   wire_packets     Solana wire-format transactions (legacy and version-0
                    messages, 1..4 signers, random account keys, blockhash
                    and instructions) in fixed-stride packet slots with a
@@ -202,6 +204,53 @@ def poh_ragged(n: int = 16384, max_hashes: int = 1_000_000, seed: int = 4):
     counts = np.floor(np.exp(rng.uniform(0.0, np.log(max_hashes + 1), n))).astype(np.uint64)
     counts = np.clip(counts, 1, max_hashes).astype(np.uint64)
     return hashes, counts
+
+
+@dataclass
+class PohEntries:
+    """Chains of Solana ledger entries: chain c starts from start[c] and
+    holds entries first[c] .. first[c + 1] - 1; entry e has num_hashes[e]
+    hashes and, when has_mixin[e], the 32-byte mixin mixins[e] (the hash of
+    its transactions).  `expected` (set by the caller from a recording) are
+    the entry hashes."""
+    start: np.ndarray
+    first: np.ndarray
+    num_hashes: np.ndarray
+    mixins: np.ndarray
+    has_mixin: np.ndarray
+    expected: np.ndarray | None = None
+
+    def entry_start(self) -> np.ndarray:
+        """The hash each entry starts from: its chain's start, else the
+        previous entry's expected hash."""
+        out = np.zeros((len(self.num_hashes), 32), dtype=np.uint8)
+        for c in range(len(self.start)):
+            a, b = int(self.first[c]), int(self.first[c + 1])
+            if b > a:
+                out[a] = self.start[c]
+                out[a + 1:b] = self.expected[a:b - 1]
+        return out
+
+
+def poh_entries(chains: int = 64, entries_per_chain: int = 80, tick_hashes: int = 12500, tx_frac: float = 0.8,
+                max_tx_hashes: int = 64, seed: int = 12) -> PohEntries:
+    """Slots of a Solana-like ledger: entries are ticks (tick_hashes hashes,
+    no mixin) or transaction entries (1..max_tx_hashes hashes, a random
+    mixin), `tx_frac` of them transaction entries; every chain opens with a
+    mixin after zero hashes and an empty tick."""
+    rng = np.random.default_rng(seed)
+    n = chains * entries_per_chain
+    first = np.arange(chains + 1, dtype=np.uint64) * entries_per_chain
+    has_mixin = (rng.random(n) < tx_frac).astype(np.uint8)
+    num_hashes = np.where(has_mixin == 1, rng.integers(1, max_tx_hashes + 1, n), tick_hashes).astype(np.uint64)
+    for c in range(chains):
+        e = c * entries_per_chain
+        if entries_per_chain >= 3:
+            num_hashes[e], has_mixin[e] = 0, 1          # a mixin with no hash before it
+            num_hashes[e + 1], has_mixin[e + 1] = 0, 0  # an empty tick: the hash is unchanged
+    mixins = rng.integers(0, 256, (n, 32), dtype=np.uint8)
+    start = rng.integers(0, 256, (chains, 32), dtype=np.uint8)
+    return PohEntries(start, first, num_hashes, mixins, has_mixin)
 
 
 def corrupt_expected(expected: np.ndarray, frac: float, seed: int):

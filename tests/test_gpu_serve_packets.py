@@ -95,7 +95,9 @@ def test_packets_in_the_mix(lib, oracle, wires):
                 exp = ver[k] if kind == "v" else sig[k] if kind == "s" else poh
                 assert np.array_equal(res, exp), (kind, k)
         kinds = {e[0] for e in srv.trace()}
-        assert 3 in kinds and 0 in kinds and 2 in kinds
+        # wire packets in slot launches (3), offset-form jobs on the resident
+        # signature service (4), PoH (2)
+        assert 3 in kinds and 4 in kinds and 2 in kinds
     finally:
         srv.close()
 
