@@ -539,6 +539,82 @@ def bench_poh_saturation(lib, torch, peaks, hashes=2000):
                                    "path": "gb300_poh_verify_batch_device (autotuned form)"}}
 
 
+def bench_poh_entries(lib, torch, nthreads, reps=3):
+    """Solana ledger entries: 64 chains x 80 entries (ticks of 12,500
+    hashes, transaction entries of 1..64 hashes with a 32-byte mixin).
+    Recording on the GPU (one thread per chain), then verification of every
+    entry on the GPU (plain hashes as one ragged PoH batch, then the mixin
+    step and the comparison), with 3% of the recorded hashes corrupted; the
+    CPU oracle checks the recording and every verdict."""
+    import workloads
+    from oracle.oracle import get_oracle
+    w = workloads.poh_entries(chains=64, entries_per_chain=80, tick_hashes=12500, seed=12)
+    n = len(w.num_hashes)
+    plain = np.where(w.has_mixin == 1, np.maximum(w.num_hashes.astype(np.int64), 1) - 1,
+                     w.num_hashes.astype(np.int64))
+    hashes = int(plain.sum()) + 2 * int(w.has_mixin.sum())        # compressions, the mixin step being two
+    stream = torch.cuda.current_stream()
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    # recording, device form
+    d_first, d_nh, d_mx, d_hm = dev(w.first.astype(np.int64)), dev(w.num_hashes.astype(np.int64)), dev(w.mixins), \
+        dev(w.has_mixin)
+    d_out = torch.zeros((n, 32), dtype=torch.uint8, device="cuda")
+    rec_t = []
+    for it in range(reps + 1):
+        d_h = dev(w.start.copy())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        lib.poh_record_device(d_h, d_first, d_nh, d_mx, d_hm, d_out, stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if it:
+            rec_t.append(e0.elapsed_time(e1) * 1e-3)
+    w.expected = d_out.cpu().numpy()
+    rng = np.random.default_rng(13)
+    exp = w.expected.copy()
+    bad = rng.random(n) < 0.03
+    exp[bad, 7] ^= 0x40
+    start = w.entry_start()
+    # verification, device form
+    d_start, d_exp = dev(start), dev(exp)
+    d_ok = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    ws = torch.empty(lib.poh_entries_workspace_size(n), dtype=torch.uint8, device="cuda")
+    ver_t = []
+    for it in range(reps + 1):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        lib.poh_verify_entries_device(d_start, d_nh, d_mx, d_hm, d_exp, d_ok, None, ws, stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if it:
+            ver_t.append(e0.elapsed_time(e1) * 1e-3)
+    ok = d_ok.cpu().numpy()
+    # host form, end to end
+    t = time.perf_counter()
+    ok_host = lib.poh_verify_entries(start, w.num_hashes, w.mixins, w.has_mixin, exp)
+    e2e_s = time.perf_counter() - t
+    o = get_oracle()
+    t = time.perf_counter()
+    ok_cpu, out_cpu = o.poh_verify_entries(start, w.num_hashes, w.mixins, w.has_mixin, exp, nthreads)
+    cpu_s = time.perf_counter() - t
+    assert np.array_equal(out_cpu, w.expected), "GPU recording differs from the oracle"
+    assert np.array_equal(ok, ok_cpu) and np.array_equal(ok_host, ok_cpu), "entry verdicts differ from the oracle"
+    assert np.array_equal(ok.astype(bool), ~bad)
+    v_s, r_s = min(ver_t), min(rec_t)
+    return {"config": {"workload": "64 chains x 80 Solana ledger entries (ticks of 12,500 hashes; 80% transaction "
+                                   "entries of 1..64 hashes with a mixin), 3% corrupted recorded hashes (seeded)",
+                       "entries": n, "sha256_compressions": hashes},
+            "verify_device": {"entries_per_s": n / v_s, "hashes_per_s": hashes / v_s, "s": v_s},
+            "verify_e2e": {"entries_per_s": n / e2e_s, "s": e2e_s,
+                           "path": "gb300_poh_verify_entries (host buffers)",
+                           "h2d_bytes_per_step": n * (32 * 3 + 9), "d2h_bytes_per_step": n},
+            "record_device": {"entries_per_s": n / r_s, "hashes_per_s": hashes / r_s, "s": r_s,
+                              "note": "one thread per chain: 64 chains occupy 64 lanes"},
+            "parity": "recording and every verdict equal the CPU oracle's",
+            "cpu_baseline": {"entries_per_s": n / cpu_s, "cores": nthreads, "kind": "port",
+                             "sample": "the full workload, CPU oracle entry verification"}}
+
+
 def bench_wire_packets(lib, torch, nthreads, n=16384, reps=5):
     """Solana wire-format packets (16384 slots of 1280 bytes; legacy and
     version-0 transactions with 1..4 signers; 5% corrupted, 3% malformed):
@@ -828,14 +904,23 @@ def bench_serving(lib, levels=(0.1, 0.25, 0.5, 0.8, 1.0, 1.2), duration_s=1.0, m
                     sig_items += items(kind, k)
                 srv.release(t)
             sig_lat = lat["v"] + lat["s"]
-            rows.append({"offered_fraction_of_peak": lv, "offered_requests_per_s": lam, "requests": n,
-                         "achieved_submit_rate": submit_rate,
-                         "sig_items_per_s": sig_items / max(1e-9, (t_last - t_first) * 1e-9),
-                         "sig_latency_ms": {"p50": _pct(sig_lat, 50) * 1e3, "p99": _pct(sig_lat, 99) * 1e3,
-                                            "p99.9": _pct(sig_lat, 99.9) * 1e3},
-                         "verify_latency_ms_p99": (_pct(lat["v"], 99) or 0) * 1e3,
-                         "poh_latency_ms": {"p50": (_pct(lat["p"], 50) or 0) * 1e3,
-                                            "p99": (_pct(lat["p"], 99) or 0) * 1e3}})
+            row = {"offered_fraction_of_peak": lv, "offered_requests_per_s": lam, "requests": n,
+                   "achieved_submit_rate": submit_rate,
+                   "sig_items_per_s": sig_items / max(1e-9, (t_last - t_first) * 1e-9),
+                   "sig_latency_ms": {"p50": _pct(sig_lat, 50) * 1e3, "p99": _pct(sig_lat, 99) * 1e3,
+                                      "p99.9": _pct(sig_lat, 99.9) * 1e3},
+                   "verify_latency_ms_p99": (_pct(lat["v"], 99) or 0) * 1e3,
+                   "poh_latency_ms": {"p50": (_pct(lat["p"], 50) or 0) * 1e3,
+                                      "p99": (_pct(lat["p"], 99) or 0) * 1e3}}
+            # resident signature service: where each request's time went on
+            # the GPU (publication to first claimed chunk, then to completion)
+            svc = [e for e in srv.trace() if e[0] == 4][-len(sig_lat):] if sig_lat else []
+            if svc:
+                row["service_gpu_ms"] = {"wait_p50": _pct([e[6] for e in svc], 50),
+                                         "wait_p99": _pct([e[6] for e in svc], 99),
+                                         "run_p50": _pct([e[7] for e in svc], 50),
+                                         "run_p99": _pct([e[7] for e in svc], 99)}
+            rows.append(row)
         stats = srv.stats()
     finally:
         srv.close()
@@ -1066,8 +1151,16 @@ def run_ours(args):
         line["poh_ragged"] = bench_poh_ragged(lib, torch, steps=2)
         line["ragged_sigs"] = bench_ragged_sigs(lib, torch)
         line["wire_packets"] = bench_wire_packets(lib, torch, nthreads)
+        line["poh_entries"] = bench_poh_entries(lib, torch, nthreads)
     if not args.skip_serving:
         line["serving"] = bench_serving(lib)
+        # the same mix with verify/sign jobs merged into slot launches instead
+        # of the resident signature service, at 80 % of that form's own peak
+        alt = bench_serving(lib, levels=(0.8,), plain_requests=0, server_kwargs={"sig_mode": 1})
+        line["serving"]["slot_launches_at_0.8"] = {"peak_requests_per_s": alt["peak_requests_per_s"],
+                                                   "level": alt["levels"][0],
+                                                   "results_identical_alone_and_in_mix":
+                                                       alt["results_identical_alone_and_in_mix"]}
     line["autotuner"] = lib.tuning()
     line["summary"] = summarize(line)           # last key: the compact view of every metric
     if rank == 0:
@@ -1108,11 +1201,24 @@ def summarize(line: dict) -> dict:
                                "served_peak": r(wp["served"]["peak_packets_per_s"]),
                                "served_p99_ms_at_0.8": r(next((x["latency_ms"]["p99"] for x in wp["served"]["levels"]
                                                                if x["offered_fraction_of_peak"] == 0.8), None))}
+    if "poh_entries" in line:
+        pe = line["poh_entries"]
+        out["poh_entries"] = {"verify_entries_per_s": r(pe["verify_device"]["entries_per_s"]),
+                              "verify_hashes_per_s": r(pe["verify_device"]["hashes_per_s"]),
+                              "cpu_entries_per_s": r(pe["cpu_baseline"]["entries_per_s"])}
     if "serving" in line:
         sv = line["serving"]
         out["serving_mix"] = {"peak_requests_per_s": r(sv["peak_requests_per_s"]),
+                              "sig_p50_ms": {str(x["offered_fraction_of_peak"]): r(x["sig_latency_ms"]["p50"], 3)
+                                             for x in sv["levels"]},
                               "sig_p99_ms": {str(x["offered_fraction_of_peak"]): r(x["sig_latency_ms"]["p99"], 3)
                                              for x in sv["levels"]}}
+        if "slot_launches_at_0.8" in sv:
+            alt = sv["slot_launches_at_0.8"]
+            out["serving_mix"]["slot_launches_at_0.8"] = {
+                "peak_requests_per_s": r(alt["peak_requests_per_s"]),
+                "sig_p50_ms": r(alt["level"]["sig_latency_ms"]["p50"], 3),
+                "sig_p99_ms": r(alt["level"]["sig_latency_ms"]["p99"], 3)}
     out["parity"] = "every section's outputs checked equal to the reference's (golden digests)"
     return out
 

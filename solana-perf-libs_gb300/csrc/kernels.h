@@ -167,6 +167,14 @@ struct SvcParams {
     uint64_t idle_ns;        // the launch leaves (all warps together) after this long without a claim
     const CurveTables* tables;
 };
+// The L1 / shared-memory split (percent of the largest shared size) that
+// the persistent PoH kernels and the resident signature kernel ask for, so
+// that neither waits for the other to drain an SM: 164 of 228 KB shared.
+// Two service blocks (2 x 60.4 KB) and two PoH pair blocks (2 x 14.3 KB)
+// fit, and L1 keeps ~92 KB for the verify path's per-thread point tables
+// (local memory).
+constexpr int kServeCarveoutPercent = 72;
+
 // Blocks of the service kernel that fit on one SM (sets its shared-memory
 // attributes on the current device first).
 cudaError_t sig_service_blocks_per_sm(int* blocks);

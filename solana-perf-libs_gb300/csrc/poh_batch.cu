@@ -401,14 +401,13 @@ __global__ void __launch_bounds__(64 * P) poh_pair_persistent_kernel(uint8_t* ha
 // placed there until the SM drains.  With the driver's own split for these
 // kernels (14 KB of shared memory per pair block), the served loop's
 // resident signature kernel (60 KB per block) could wait behind running PoH
-// launches.  The chains live in registers and use no L1, so these kernels
-// ask for the largest shared-memory split, as the resident signature kernel
-// does.
+// launches.  These kernels and that one therefore ask for one split,
+// kServeCarveoutPercent of the maximum (sig_service.cu gives the sizes).
 cudaError_t preload_poh_batch_kernels() {
     cudaError_t e = load_kernels(poh_hist_kernel, poh_scan_kernel, poh_scatter_kernel, poh_choose_kernel,
                                  poh_requeue_kernel, poh_persistent_kernel<1>, poh_persistent_kernel<4>,
                                  poh_pair_persistent_kernel<1>, poh_pair_persistent_kernel<2>);
-    const int pref = cudaSharedmemCarveoutMaxShared;
+    const int pref = kServeCarveoutPercent;
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(poh_persistent_kernel<1>, cudaFuncAttributePreferredSharedMemoryCarveout, pref);
     if (e == cudaSuccess)

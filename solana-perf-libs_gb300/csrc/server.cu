@@ -588,11 +588,14 @@ int svc_try_submit(gb300_server* sv, const Req& r) {
     const uint64_t n = r.n;
     const bool verify = r.kind == 0;
     // four lanes per signature while the verifies in flight leave the GPU
-    // idle (the size rule of the one-call form: up to 64 per SM)
+    // idle (the size rule of the one-call form: up to 64 per SM);
+    // GB300_CRYPT_VERIFY_FORM = 0 / 1 forces one form, as everywhere
+    static const int forced = getenv("GB300_CRYPT_VERIFY_FORM") ? atoi(getenv("GB300_CRYPT_VERIFY_FORM")) : -1;
     uint64_t v_inflight = 0;
     for (const SvcInflight& f : V.inflight)
         if (f.kind == 0) v_inflight += f.n;
-    const bool quad = verify && v_inflight + n <= 64ull * (uint64_t)sv->info.sms;
+    const bool quad = verify && (forced == kVerifyQuad ||
+                                 (forced != kVerifySingle && v_inflight + n <= 64ull * (uint64_t)sv->info.sms));
     const uint32_t per = quad ? 8u : 32u;
     const uint64_t nchunks = (n + per - 1) / per;
     const uint64_t idx_bytes = 16 * n, pk_off = round_up(idx_bytes, 256);

@@ -98,38 +98,66 @@ __device__ __forceinline__ S ld_volatile_struct(const S* p) {
     return s;
 }
 
-// Lane 0: the next published chunk, claimed; false once the launch is
-// leaving: `exiting` set, or set here because the FIFO is empty and no warp
-// has claimed for idle_ns (or `stop` is set).  Polls device memory only,
-// backing off from 256 ns to 4 us between looks.
-__device__ __forceinline__ bool claim_chunk(const SvcParams& p, uint32_t& c, uint64_t t_start) {
+// The next published chunk, claimed for the warp; false once the launch is
+// leaving.  Polls device memory only, backing off from 256 ns to 4 us
+// between looks.  Called by the whole warp: lane 0 makes each attempt as
+// straight-line code, the outcome is broadcast, and the loop (sleeps
+// included) runs on every lane, so the warp leaves it converged.  With the
+// polling loop inside a lane-0-only branch, lanes 1-31 went ahead without
+// lane 0 and the warp stayed split in two for the whole chunk: measured on
+// GB300 with ncu, the four-lane verify then issued twice its instructions
+// with ~20 active threads and 2.6 branch-resolution stalls per issue, and
+// eight signatures took 3.0 ms against 0.46 ms in a plain launch.
+__device__ __forceinline__ bool claim_chunk(const SvcParams& p, uint32_t lane, uint32_t& c, uint64_t t_start) {
     uint32_t sleep_ns = 256;
     for (;;) {
-        if (ld_relaxed_gpu(&p.dev->exiting)) return false;
-        const uint32_t t = ld_relaxed_gpu(&p.dev->tail);
-        const uint32_t h = ld_relaxed_gpu(&p.dev->head);
-        if ((int32_t)(t - h) > 0) {
-            if (atomicCAS(&p.dev->head, h, h + 1u) == h) {
-                c = h;
-                atomicMax(reinterpret_cast<unsigned long long*>(&p.dev->last_claim_ns),
-                          (unsigned long long)global_ns());
-                return true;
+        uint32_t r = 3, got = 0;      // 0 leave, 1 claimed, 2 lost a race (look again), 3 empty
+        if (lane == 0) {
+            if (ld_relaxed_gpu(&p.dev->exiting)) {
+                r = 0;
+            } else {
+                const uint32_t t = ld_relaxed_gpu(&p.dev->tail);
+                const uint32_t h = ld_relaxed_gpu(&p.dev->head);
+                if ((int32_t)(t - h) > 0) {
+                    if (atomicCAS(&p.dev->head, h, h + 1u) == h) {
+                        r = 1;
+                        got = h;
+                        atomicMax(reinterpret_cast<unsigned long long*>(&p.dev->last_claim_ns),
+                                  (unsigned long long)global_ns());
+                    } else {
+                        r = 2;
+                    }
+                } else {
+                    const uint64_t last = ld_relaxed_gpu64(&p.dev->last_claim_ns);
+                    const uint64_t since = last > t_start ? last : t_start;
+                    const uint64_t now = global_ns();
+                    if (ld_relaxed_gpu(&p.dev->stop) || (now > since && now - since > p.idle_ns)) {
+                        atomicExch(&p.dev->exiting, 1u);
+                        r = 0;
+                    }
+                }
             }
-            continue;                                   // another warp took it: look again at once
         }
-        const uint64_t last = ld_relaxed_gpu64(&p.dev->last_claim_ns);
-        const uint64_t since = last > t_start ? last : t_start;
-        if (ld_relaxed_gpu(&p.dev->stop) || global_ns() - since > p.idle_ns) {
-            atomicExch(&p.dev->exiting, 1u);
-            return false;
+        r = __shfl_sync(0xffffffffu, r, 0);
+        if (r == 0) return false;
+        if (r == 1) {
+            c = __shfl_sync(0xffffffffu, got, 0);
+            return true;
         }
-        __nanosleep(sleep_ns);
-        if (sleep_ns < 4096) sleep_ns <<= 1;
+        if (r == 3) {
+            __nanosleep(sleep_ns);
+            if (sleep_ns < 4096) sleep_ns <<= 1;
+        }
     }
 }
 
-template <int T, int W, int MINB>
-__global__ void __launch_bounds__(T, MINB) sig_service_kernel(SvcParams p) {
+// At most 216 registers a thread (__maxnreg__, which excludes
+// __launch_bounds__; launched with 128 threads): the four-lane verify keeps
+// its registers without spilling, and two blocks per SM (55,296 registers)
+// leave room for the PoH pair blocks that run beside them.  A 168-register
+// build (three blocks per SM) spilled in the four-lane path.
+template <int T, int W>
+__global__ void __maxnreg__(216) sig_service_kernel(SvcParams p) {
     __shared__ uint32_t sVB[VB_WORDS * VB_ENTRIES];
     extern __shared__ uint4 s_comb4[];
     for (int k = threadIdx.x; k < VB_WORDS * VB_ENTRIES; k += blockDim.x) sVB[k] = p.tables->vb[k];
@@ -143,11 +171,8 @@ __global__ void __launch_bounds__(T, MINB) sig_service_kernel(SvcParams p) {
     const uint64_t t_start = global_ns();
     if (lane == 0) atomicAdd(&p.dev->warps, 1u);
     for (;;) {
-        uint32_t c = 0, got = 0;
-        if (lane == 0) got = claim_chunk(p, c, t_start) ? 1u : 0u;
-        got = __shfl_sync(0xffffffffu, got, 0);
-        if (!got) break;
-        c = __shfl_sync(0xffffffffu, c, 0);
+        uint32_t c = 0;
+        if (!claim_chunk(p, lane, c, t_start)) break;
         // every lane synchronises with the publication of chunk c (the
         // stream write of tail after the input copies): its later loads of
         // the descriptors (host memory) and inputs (device memory) see them
@@ -192,9 +217,7 @@ __global__ void __launch_bounds__(T, MINB) sig_service_kernel(SvcParams p) {
     }
 }
 
-// 168 registers (3 blocks of 128 per SM fit); the server runs fewer so
-// that PoH launches keep room beside it.
-#define SVC_KERNEL sig_service_kernel<kSvcThreads, 4, 3>
+#define SVC_KERNEL sig_service_kernel<kSvcThreads, 4>
 
 // %globaltimer now, for relating the kernel's times to the host clock.
 __global__ void svc_clock_kernel(uint64_t* out) { *reinterpret_cast<volatile uint64_t*>(out) = global_ns(); }
@@ -219,8 +242,8 @@ cudaError_t sig_service_blocks_per_sm(int* blocks) {
         if (e != cudaSuccess) return e;
         // the same L1 / shared split as the PoH kernels it runs beside
         // (poh_batch.cu), so neither waits for the other to drain an SM
-        e = cudaFuncSetAttribute(SVC_KERNEL, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 cudaSharedmemCarveoutMaxShared);
+        // (kernels.h gives the sizes)
+        e = cudaFuncSetAttribute(SVC_KERNEL, cudaFuncAttributePreferredSharedMemoryCarveout, kServeCarveoutPercent);
         if (e != cudaSuccess) return e;
         opted.fetch_or(bit);
     }
