@@ -42,12 +42,21 @@ int gb300_poh_verify_batch_shape(uint8_t* hashes, const uint64_t* num_hashes, ui
 /* gb300_ed25519_verify_device with the kernel form forced instead of picked
  * by batch size: form 0 one thread per signature (the tuned window width of
  * h), 1 four lanes per signature, 2 one thread per signature with a 4-bit
- * window, 3 the same with a 5-bit window.  Same verdicts in every form; used
- * to test and time each.  Returns a cudaError_t. */
+ * window, 3 the same with a 5-bit window, 4 three warps per eight
+ * signatures with half-size scalars.  Same verdicts in every form; used to test and
+ * time each.  Returns a cudaError_t. */
 int gb300_ed25519_verify_device_form(const uint8_t* packets, uint64_t packets_len, const uint32_t* message_lens,
                                      const uint32_t* public_key_offsets, const uint32_t* signature_offsets,
                                      const uint32_t* message_start_offsets, uint32_t num, uint8_t* out, int form,
                                      void* stream);
+
+/* The half-size scalars the three-warp verify form uses: for each of `num`
+ * values h < L (8 little-endian 32-bit words each, device memory) writes 18
+ * words to `out` (device memory): |c| (8 words), all ones when c < 0 else 0,
+ * d (8 words), and the rounds of the lattice reduction; c = d h (mod 8L)
+ * with d odd and positive, (c, d) = (h, 1) when no short pair fits.  Used
+ * to test the reduction on chosen h.  Returns a cudaError_t. */
+int gb300_diag_half_scalars(const uint32_t* h, uint32_t num, uint32_t* out, void* stream);
 
 #ifdef __cplusplus
 }

@@ -45,7 +45,7 @@ cudaError_t preload_packets_kernels();
 // Ed25519 verify: out[i] = 1 if signature i is valid under the reference's
 // acceptance rules, else 0.  Forms: one thread per signature, or four lanes
 // per signature (lower latency on batches that do not fill the GPU).
-enum VerifyForm : int { kVerifySingle = 0, kVerifyQuad = 1 };
+enum VerifyForm : int { kVerifySingle = 0, kVerifyQuad = 1, kVerifyTrio = 2 };
 cudaError_t launch_ed25519_verify(const SigBatch& b, cudaStream_t s);
 cudaError_t launch_ed25519_verify_form(const SigBatch& b, cudaStream_t s, int form);
 
@@ -58,6 +58,9 @@ cudaError_t launch_ed25519_keypair(const uint8_t* seeds, uint8_t* pk, uint8_t* s
                                    const CurveTables* tables, cudaStream_t s);
 
 // 0 = decodes and has order not dividing 4 (reference verify.cu:88-103).
+// The half-size scalars of n values h < L (verify_trio.cuh, half_scalar.cuh):
+// 18 words per value into out (diagnostic; gb300_diag.h).
+cudaError_t launch_half_scalars(const uint32_t* h, uint32_t n, uint32_t* out, cudaStream_t s);
 cudaError_t launch_check_small_order(const uint8_t* points, uint8_t* out, uint32_t n,
                                      const CurveTables* tables, cudaStream_t s);
 

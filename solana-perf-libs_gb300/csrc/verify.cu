@@ -21,6 +21,11 @@
 // (table of 0..128 times B in shared memory).  Fixed windows keep a warp in
 // lock-step: every lane adds at the same iterations (a sliding window, as in
 // the reference, makes nearly every iteration an add for some lane).
+//
+// Batches that leave the GPU idle take a shorter chain per signature: four
+// lanes per signature (verify_quad.cuh), or three warps per eight
+// signatures with half-size scalars (verify_trio.cuh); the form is picked by
+// batch size (launch_ed25519_verify).
 #include <cuda_runtime.h>
 #include <cstdlib>
 #include "kernels.h"
@@ -39,6 +44,7 @@ namespace {
 
 #include "ed25519_ops.cuh"
 #include "verify_quad.cuh"
+#include "verify_trio.cuh"
 
 // MINB: blocks per SM the register allocation must allow.  1 lets the
 // compiler keep everything in registers (254; 2 blocks of 128 fit); 4 caps
@@ -68,6 +74,51 @@ __global__ void __launch_bounds__(VERIFY_THREADS, VERIFY_MIN_BLOCKS) ed25519_ver
     if (q == 0) a.out[i] = ok ? 1 : 0;
 }
 
+// Three warps per eight signatures (verify_trio.cuh): warps 3g, 3g + 1,
+// 3g + 2 of a block are trio g's verifier, hasher and R worker; signature
+// 8 t + l / 4 of trio t on lane l % 4 of each.  Trios past the end of the
+// batch repeat its last signature (results dropped), so every warp of
+// every trio reaches every barrier.
+template <int G>
+__global__ void __launch_bounds__(96 * G) ed25519_verify_trio_kernel(SigBatch a) {
+    __shared__ TrioShare sh[G];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t trio = warp / 3u, role = warp - 3u * trio;
+    const uint64_t gi = ((uint64_t)blockIdx.x * G + trio) * 8u + (lane >> 2);
+    const uint32_t i = gi < a.n ? (uint32_t)gi : a.n - 1u;
+    const uint32_t bar = 1u + 4u * trio;                     // named barriers bar .. bar + 3 (0 is __syncthreads)
+    if (role == 0) {
+        const bool ok = trio_verifier(a, sh[trio], i, lane, bar);
+        if (gi < a.n && (lane & 3u) == 0) a.out[gi] = ok ? 1 : 0;
+    } else if (role == 1) {
+        trio_hasher(a, sh[trio], i, lane, bar);
+    } else {
+        trio_r_worker(a, sh[trio], lane, bar);
+    }
+}
+
+// The half-size scalars of each h (8 words < L) into out[18 i ..]: |c| (8
+// words), c's sign (all ones when negative), d (8 words), the reduction's
+// rounds.  Whole warps run (half_scalars votes over the warp); lanes past n
+// take h = 0 and write nothing.
+__global__ void half_scalars_kernel(const uint32_t* h, uint32_t n, uint32_t* out) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t x[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) x[k] = i < n ? h[8 * i + k] : 0u;
+    hs::HalfScalars r;
+    hs::half_scalars(r, x);
+    if (i >= n) return;
+    uint32_t* o = out + 18 * i;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        o[k] = r.c[k];
+        o[9 + k] = r.d[k];
+    }
+    o[8] = r.cneg;
+    o[17] = r.rounds;
+}
+
 // 0 = the encoding decodes and is not of order dividing 4.
 __global__ void check_small_order_kernel(const uint8_t* pts, uint8_t* out, uint32_t n, const CurveTables* T) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -85,11 +136,27 @@ __global__ void check_small_order_kernel(const uint8_t* pts, uint8_t* out, uint3
 cudaError_t preload_verify_kernels() {
     return load_kernels(ed25519_verify_kernel<4, VERIFY_MIN_BLOCKS>, ed25519_verify_kernel<4, 4>,
                         ed25519_verify_kernel<5, VERIFY_MIN_BLOCKS>, ed25519_verify_quad_kernel,
+                        ed25519_verify_trio_kernel<1>, ed25519_verify_trio_kernel<2>, half_scalars_kernel,
                         check_small_order_kernel);
 }
 
 cudaError_t launch_ed25519_verify_form(const SigBatch& b, cudaStream_t s, int form) {
     if (b.n == 0) return cudaSuccess;
+    if (form == kVerifyTrio) {
+        // one trio per block (its three warps on three sub-partitions of an
+        // SM) while that fits the SMs once, else two
+        int dev = 0, sms = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            return cudaGetLastError();
+        const uint64_t trios = (b.n + 7ull) / 8ull;
+        if (trios <= (uint64_t)sms) {
+            ed25519_verify_trio_kernel<1><<<(unsigned)trios, 96, 0, s>>>(b);
+        } else {
+            ed25519_verify_trio_kernel<2><<<(unsigned)((trios + 1) / 2), 192, 0, s>>>(b);
+        }
+        return cudaGetLastError();
+    }
     if (form == kVerifyQuad) {
         const uint64_t threads = 4ull * b.n;
         if (threads > 0xffffffffull) return cudaErrorInvalidValue;
@@ -113,14 +180,20 @@ cudaError_t launch_ed25519_verify_form(const SigBatch& b, cudaStream_t s, int fo
     return cudaGetLastError();
 }
 
-// Form by batch size: four lanes per signature while the batch leaves the
-// GPU idle (measured on GB300: 1,024 signatures 0.49 ms against 0.98 ms;
-// 8,192: 0.69 against 0.98; break-even near 12,000 = 78 per SM, above which
-// one thread per signature has the throughput: 116,736 in 4.6 ms against
-// 8.0).  GB300_CRYPT_VERIFY_FORM = 0 / 1 forces a form.
+// Form by batch size, measured on GB300 (L2 flushed between launches):
+//   * three warps per eight signatures up to 40 per SM (6,080): 1,024
+//     signatures in 0.28 ms against 0.51 (four lanes) and 1.02 (one lane);
+//     4,096 in 0.41 against 0.53; 6,144 in 0.67 against 0.70;
+//   * four lanes per signature up to 64 per SM (9,728): 0.72 ms against
+//     1.02; break-even with one lane near 12,000 = 78 per SM;
+//   * one thread per signature above, where throughput counts: 116,736 in
+//     4.6 ms against 8.0 for four lanes.
+// GB300_CRYPT_VERIFY_FORM = 0 / 1 / 2 forces one lane / four lanes / three
+// warps.
 cudaError_t launch_ed25519_verify(const SigBatch& b, cudaStream_t s) {
     static const int forced = getenv("GB300_CRYPT_VERIFY_FORM") ? atoi(getenv("GB300_CRYPT_VERIFY_FORM")) : -1;
-    if (forced == kVerifySingle || forced == kVerifyQuad) return launch_ed25519_verify_form(b, s, forced);
+    if (forced == kVerifySingle || forced == kVerifyQuad || forced == kVerifyTrio)
+        return launch_ed25519_verify_form(b, s, forced);
     static int sms_cache[64];
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return cudaGetLastError();
@@ -129,8 +202,15 @@ cudaError_t launch_ed25519_verify(const SigBatch& b, cudaStream_t s) {
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return cudaGetLastError();
         if (dev >= 0 && dev < 64) __atomic_store_n(&sms_cache[dev], sms, __ATOMIC_RELAXED);
     }
-    const int form = (uint64_t)b.n <= 64ull * (uint64_t)sms ? kVerifyQuad : kVerifySingle;
+    const uint64_t n = b.n, m = (uint64_t)sms;
+    const int form = n <= 40ull * m ? kVerifyTrio : n <= 64ull * m ? kVerifyQuad : kVerifySingle;
     return launch_ed25519_verify_form(b, s, form);
+}
+
+cudaError_t launch_half_scalars(const uint32_t* h, uint32_t n, uint32_t* out, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    half_scalars_kernel<<<(n + 127) / 128, 128, 0, s>>>(h, n, out);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_check_small_order(const uint8_t* points, uint8_t* out, uint32_t n, const CurveTables* tables,

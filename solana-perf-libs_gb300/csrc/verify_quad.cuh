@@ -146,11 +146,12 @@ __device__ __forceinline__ void qadd_cached(ge_done& r, const ge_p3& p, const fe
     qadd_finish(r, m, neg, mask);
 }
 
-// p +- (entry e of the basepoint table in shared memory): lane 0 reads y-x
-// (y+x when subtracting), lane 1 y+x (y-x), lane 2 2dxy, lane 3 multiplies
-// Z by 2 (the affine addend has Z = 1).
-__device__ __forceinline__ void qadd_niels(ge_done& r, const ge_p3& p, const uint32_t* sVB, int e, bool neg,
-                                           const QuadSel& q, uint32_t lane_q, uint32_t mask) {
+// p +- n for an affine point n in niels form (y+x, y-x, 2dxy), word k of
+// component j at n[(8 j + k) * stride]: lane 0 reads y-x (y+x when
+// subtracting), lane 1 y+x (y-x), lane 2 2dxy, lane 3 multiplies Z by 2
+// (the affine addend has Z = 1).
+__device__ __forceinline__ void qadd_niels_at(ge_done& r, const ge_p3& p, const uint32_t* n, int stride, bool neg,
+                                              const QuadSel& q, uint32_t lane_q, uint32_t mask) {
     fe ypx, ymx, o1, o2, m;
     fe_add(ypx, p.Y, p.X);
     fe_sub(ymx, p.Y, p.X);
@@ -162,11 +163,17 @@ __device__ __forceinline__ void qadd_niels(ge_done& r, const ge_p3& p, const uin
     const uint32_t two0 = 2u & q.m3;
 #pragma unroll
     for (int w = 0; w < 8; w++) {
-        const uint32_t v = sVB[(comp * 8 + w) * VB_ENTRIES + e];
+        const uint32_t v = n[(comp * 8 + w) * stride];
         o2.v[w] = (v & ~q.m3) | (w == 0 ? two0 : 0u);
     }
     fe_mul(m, o1, o2);
     qadd_finish(r, m, neg, mask);
+}
+
+// p +- (entry e of the basepoint table in shared memory, word-major)
+__device__ __forceinline__ void qadd_niels(ge_done& r, const ge_p3& p, const uint32_t* sVB, int e, bool neg,
+                                           const QuadSel& q, uint32_t lane_q, uint32_t mask) {
+    qadd_niels_at(r, p, sVB + e, VB_ENTRIES, neg, q, lane_q, mask);
 }
 
 // This lane's two components of the cached form of P.
@@ -178,6 +185,48 @@ __device__ __forceinline__ void qcached_comps(fe& c0, fe& c1, const ge_p3& P, co
     fe_mul(t2d, P.T, d2);
     fe_pick4(c0, ymx, ypx, t2d, z2, q);
     fe_pick4(c1, ypx, ymx, t2d, z2, q);
+}
+
+// This lane's components of k P for k = 0..8, P = (x, y) affine: entry k
+// holds (c0, c1) of the cached form (see qadd_cached).
+__device__ __forceinline__ void quad_table(fe tq[9][2], const fe& x, const fe& y, const fe& d2, const QuadSel& q,
+                                           uint32_t mask) {
+    ge_p3 P1, P2, P3, P4, t3;
+    ge_done t;
+    P1.X = x;
+    P1.Y = y;
+    fe_set(P1.Z, 1);
+    fe_mul(P1.T, x, y);
+    {
+        fe one, two, zero;
+        fe_set(one, 1);
+        fe_set(two, 2);
+        fe_set(zero, 0);
+        fe_pick4(tq[0][0], one, one, zero, two, q);
+        tq[0][1] = tq[0][0];
+    }
+    qcached_comps(tq[1][0], tq[1][1], P1, d2, q);
+    qdbl(t, P1.X, P1.Y, P1.Z, q, mask);
+    qto_p3(P2, t, q, mask);
+    qcached_comps(tq[2][0], tq[2][1], P2, d2, q);
+    qadd_cached(t, P2, tq[1][0], tq[1][1], false, q, mask);
+    qto_p3(P3, t, q, mask);
+    qcached_comps(tq[3][0], tq[3][1], P3, d2, q);
+    qdbl(t, P2.X, P2.Y, P2.Z, q, mask);
+    qto_p3(P4, t, q, mask);
+    qcached_comps(tq[4][0], tq[4][1], P4, d2, q);
+    qadd_cached(t, P4, tq[1][0], tq[1][1], false, q, mask);
+    qto_p3(t3, t, q, mask);
+    qcached_comps(tq[5][0], tq[5][1], t3, d2, q);
+    qdbl(t, P3.X, P3.Y, P3.Z, q, mask);
+    qto_p3(t3, t, q, mask);
+    qcached_comps(tq[6][0], tq[6][1], t3, d2, q);
+    qadd_cached(t, t3, tq[1][0], tq[1][1], false, q, mask);
+    qto_p3(t3, t, q, mask);
+    qcached_comps(tq[7][0], tq[7][1], t3, d2, q);
+    qdbl(t, P4.X, P4.Y, P4.Z, q, mask);
+    qto_p3(t3, t, q, mask);
+    qcached_comps(tq[8][0], tq[8][1], t3, d2, q);
 }
 
 // 32-byte encoding with y (low 255 bits) < p
@@ -240,45 +289,7 @@ __device__ bool verify_quad(const SigBatch& a, const uint32_t* sVB, uint32_t i, 
 
     // this lane's components of k(-A), k = 0..8
     fe tq[9][2];
-    {
-        const fe d2 = K.d2;
-        ge_p3 P1, P2, P3, P4, t3;
-        ge_done t;
-        P1.X = ax;
-        P1.Y = ay;
-        fe_set(P1.Z, 1);
-        fe_mul(P1.T, ax, ay);
-        {
-            fe one, two, zero;
-            fe_set(one, 1);
-            fe_set(two, 2);
-            fe_set(zero, 0);
-            fe_pick4(tq[0][0], one, one, zero, two, q);
-            tq[0][1] = tq[0][0];
-        }
-        qcached_comps(tq[1][0], tq[1][1], P1, d2, q);
-        qdbl(t, P1.X, P1.Y, P1.Z, q, mask);
-        qto_p3(P2, t, q, mask);
-        qcached_comps(tq[2][0], tq[2][1], P2, d2, q);
-        qadd_cached(t, P2, tq[1][0], tq[1][1], false, q, mask);
-        qto_p3(P3, t, q, mask);
-        qcached_comps(tq[3][0], tq[3][1], P3, d2, q);
-        qdbl(t, P2.X, P2.Y, P2.Z, q, mask);
-        qto_p3(P4, t, q, mask);
-        qcached_comps(tq[4][0], tq[4][1], P4, d2, q);
-        qadd_cached(t, P4, tq[1][0], tq[1][1], false, q, mask);
-        qto_p3(t3, t, q, mask);
-        qcached_comps(tq[5][0], tq[5][1], t3, d2, q);
-        qdbl(t, P3.X, P3.Y, P3.Z, q, mask);
-        qto_p3(t3, t, q, mask);
-        qcached_comps(tq[6][0], tq[6][1], t3, d2, q);
-        qadd_cached(t, t3, tq[1][0], tq[1][1], false, q, mask);
-        qto_p3(t3, t, q, mask);
-        qcached_comps(tq[7][0], tq[7][1], t3, d2, q);
-        qdbl(t, P4.X, P4.Y, P4.Z, q, mask);
-        qto_p3(t3, t, q, mask);
-        qcached_comps(tq[8][0], tq[8][1], t3, d2, q);
-    }
+    quad_table(tq, ax, ay, K.d2, q, mask);
 
     uint32_t hh[8], ss[8];
 #pragma unroll

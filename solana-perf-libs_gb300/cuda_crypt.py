@@ -144,6 +144,8 @@ class CudaCrypt:
         L.gb300_ed25519_verify_device_form.argtypes = [ctypes.c_void_p, ctypes.c_uint64] + [ctypes.c_void_p] * 4 + \
             [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         L.gb300_ed25519_verify_device_form.restype = ctypes.c_int
+        L.gb300_diag_half_scalars.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p]
+        L.gb300_diag_half_scalars.restype = ctypes.c_int
 
     # ---- reference entry points ------------------------------------------
     def init(self) -> bool:
@@ -436,7 +438,7 @@ class CudaCrypt:
         if rc != 0:
             raise RuntimeError(f"gb300_ed25519_verify_device: cudaError {rc}")
 
-    VERIFY_SINGLE, VERIFY_QUAD, VERIFY_SINGLE_W4, VERIFY_SINGLE_W5 = 0, 1, 2, 3
+    VERIFY_SINGLE, VERIFY_QUAD, VERIFY_SINGLE_W4, VERIFY_SINGLE_W5, VERIFY_TRIO = 0, 1, 2, 3, 4
 
     def verify_device_form(self, packets, message_lens, public_key_offsets, signature_offsets,
                            message_start_offsets, out, form, stream=0) -> None:
@@ -447,6 +449,13 @@ class CudaCrypt:
             out.data_ptr(), form, stream)
         if rc != 0:
             raise RuntimeError(f"gb300_ed25519_verify_device_form: cudaError {rc}")
+
+    def half_scalars_device(self, h, out, stream=0) -> None:
+        """The three-warp verify form's half-size scalars of h (uint32 tensor
+        [n, 8]) into out (uint32 tensor [n, 18]) (diagnostic)."""
+        rc = self.lib.gb300_diag_half_scalars(h.data_ptr(), h.shape[0], out.data_ptr(), stream)
+        if rc != 0:
+            raise RuntimeError(f"gb300_diag_half_scalars: cudaError {rc}")
 
     def sign_device(self, packets, message_lens, public_key_offsets, private_key_offsets, message_start_offsets,
                     out, stream=0) -> None:
