@@ -769,7 +769,7 @@ int gb300_ed25519_verify_device_form(const uint8_t* packets, uint64_t packets_le
                                      const uint32_t* message_start_offsets, uint32_t num, uint8_t* out, int form,
                                      void* stream) {
     if (num == 0) return 0;
-    if (form < 0 || form > 4) return (int)cudaErrorInvalidValue;
+    if (form < 0 || form > 5) return (int)cudaErrorInvalidValue;
     Device* D = current_device();
     if (!D) return (int)cudaErrorNoDevice;
     if (reinterpret_cast<uintptr_t>(packets) & 3u) return (int)cudaErrorMisalignedAddress;
@@ -777,7 +777,7 @@ int gb300_ed25519_verify_device_form(const uint8_t* packets, uint64_t packets_le
                message_start_offsets, num, out, D->tables};
     b.window = form == 2 ? 4 : form == 3 ? 5 : verify_window_if_tuned(*D);
     return (int)launch_ed25519_verify_form(b, static_cast<cudaStream_t>(stream),
-                                           form == 1 ? kVerifyQuad : form == 4 ? kVerifyTrio : kVerifySingle);
+                                           form == 1 ? kVerifyQuad : form == 4 ? kVerifyTrio : form == 5 ? kVerifyStaged : kVerifySingle);
 }
 
 int gb300_diag_half_scalars(const uint32_t* h, uint32_t num, uint32_t* out, void* stream) {

@@ -53,7 +53,24 @@ __device__ __forceinline__ void load_vb(ge_niels& n, const uint32_t* sVB, int e)
     }
 }
 
-__device__ bool verify_one(const SigBatch& a, const uint32_t* sVB, uint32_t i) {
+// The signature's 16 words and the public key's 8: read from the packets,
+// or taken from `staged` (the same 24 words, staged by the caller).
+__device__ __forceinline__ void load_sig_pk(uint32_t sig[16], uint32_t pk[8], const SigBatch& a, uint64_t so,
+                                            uint64_t po, const uint32_t* staged) {
+    if (staged) {
+#pragma unroll
+        for (int k = 0; k < 16; k++) sig[k] = staged[k];
+#pragma unroll
+        for (int k = 0; k < 8; k++) pk[k] = staged[16 + k];
+        return;
+    }
+#pragma unroll
+    for (int k = 0; k < 16; k++) sig[k] = ld_u32_any(a.packets, so + 4 * k, a.packets_len);
+#pragma unroll
+    for (int k = 0; k < 8; k++) pk[k] = ld_u32_any(a.packets, po + 4 * k, a.packets_len);
+}
+
+__device__ bool verify_one(const SigBatch& a, const uint32_t* sVB, uint32_t i, const uint32_t* staged = nullptr) {
     const uint64_t so = a.signature_offsets[i];
     const uint64_t po = a.public_key_offsets[i];
     const uint64_t mo = a.message_start_offsets[i];
@@ -61,10 +78,7 @@ __device__ bool verify_one(const SigBatch& a, const uint32_t* sVB, uint32_t i) {
     if (so + 64 > a.packets_len || po + 32 > a.packets_len || mo + m > a.packets_len) return false;
 
     uint32_t sig[16], pk[8];
-#pragma unroll
-    for (int k = 0; k < 16; k++) sig[k] = ld_u32_any(a.packets, so + 4 * k, a.packets_len);
-#pragma unroll
-    for (int k = 0; k < 8; k++) pk[k] = ld_u32_any(a.packets, po + 4 * k, a.packets_len);
+    load_sig_pk(sig, pk, a, so, po, staged);
 
     if (sig[15] & 0xf0000000u) return false;               // S >= 2^252
     if (enc_is_order4(sig) || enc_is_order4(pk)) return false;
@@ -212,7 +226,7 @@ __device__ __forceinline__ uint64_t radixw_carries(const uint32_t h[8]) {
 // bit, the k(-A) addend at multiples of W, the basepoint addend (radix 256,
 // shared-memory table) at multiples of 8.  Same verdicts as verify_one.
 template <int W>
-__device__ bool verify_one_w(const SigBatch& a, const uint32_t* sVB, uint32_t i) {
+__device__ bool verify_one_w(const SigBatch& a, const uint32_t* sVB, uint32_t i, const uint32_t* staged = nullptr) {
     constexpr int NDIG = (253 + W - 1) / W;       // digits of h
     constexpr int NTAB = (1 << (W - 1)) + 1;      // k(-A), k = 0..2^(W-1)
     constexpr int TOP = W * (NDIG - 1);
@@ -223,10 +237,7 @@ __device__ bool verify_one_w(const SigBatch& a, const uint32_t* sVB, uint32_t i)
     if (so + 64 > a.packets_len || po + 32 > a.packets_len || mo + m > a.packets_len) return false;
 
     uint32_t sig[16], pk[8];
-#pragma unroll
-    for (int k = 0; k < 16; k++) sig[k] = ld_u32_any(a.packets, so + 4 * k, a.packets_len);
-#pragma unroll
-    for (int k = 0; k < 8; k++) pk[k] = ld_u32_any(a.packets, po + 4 * k, a.packets_len);
+    load_sig_pk(sig, pk, a, so, po, staged);
     if (sig[15] & 0xf0000000u) return false;               // S >= 2^252
     if (enc_is_order4(sig) || enc_is_order4(pk)) return false;
 
@@ -328,9 +339,10 @@ __device__ bool verify_one_w(const SigBatch& a, const uint32_t* sVB, uint32_t i)
 
 // verdict of signature i with window width W (4: verify_one)
 template <int W>
-__device__ __forceinline__ bool verify_window(const SigBatch& a, const uint32_t* sVB, uint32_t i) {
-    if constexpr (W == 4) return verify_one(a, sVB, i);
-    else return verify_one_w<W>(a, sVB, i);
+__device__ __forceinline__ bool verify_window(const SigBatch& a, const uint32_t* sVB, uint32_t i,
+                                              const uint32_t* staged = nullptr) {
+    if constexpr (W == 4) return verify_one(a, sVB, i, staged);
+    else return verify_one_w<W>(a, sVB, i, staged);
 }
 
 // [a]B for a < 2^255 (little-endian words), result in extended coordinates.

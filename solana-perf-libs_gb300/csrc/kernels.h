@@ -45,7 +45,7 @@ cudaError_t preload_packets_kernels();
 // Ed25519 verify: out[i] = 1 if signature i is valid under the reference's
 // acceptance rules, else 0.  Forms: one thread per signature, or four lanes
 // per signature (lower latency on batches that do not fill the GPU).
-enum VerifyForm : int { kVerifySingle = 0, kVerifyQuad = 1, kVerifyTrio = 2 };
+enum VerifyForm : int { kVerifySingle = 0, kVerifyQuad = 1, kVerifyTrio = 2, kVerifyStaged = 3 };
 cudaError_t launch_ed25519_verify(const SigBatch& b, cudaStream_t s);
 cudaError_t launch_ed25519_verify_form(const SigBatch& b, cudaStream_t s, int form);
 

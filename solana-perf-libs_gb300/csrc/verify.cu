@@ -61,6 +61,97 @@ __global__ void __launch_bounds__(VERIFY_THREADS, MINB) ed25519_verify_kernel(Si
     a.out[i] = verify_window<W>(a, sVB, i) ? 1 : 0;
 }
 
+// Packet staging for the one-lane kernel: each warp brings the 64-byte
+// signatures and 32-byte public keys of its 32 signatures on chip with
+// coalesced 16-byte loads and hands each lane its 24 words.
+//   * The aligned 16-byte chunks covering a signature (5) and a key (3) are
+//     loaded by the whole warp, lane l taking chunk l % 8 of signature
+//     4 r + l / 8 in round r (8 rounds), so the 8 lanes of one signature read
+//     its 128 bytes together and neighbouring signatures' bytes are
+//     neighbours in the packet buffer.
+//   * Chunks are written transposed into a per-warp area of shared memory,
+//     word k of signature s at raw[k * 33 + s] (structure of arrays; the
+//     stride of 33 keeps both the writes and each lane's reads of its own
+//     column free of bank conflicts).
+//   * Each lane then assembles its signature's and key's words from its
+//     column, shifting by the byte offset of the signature within its first
+//     chunk (packets need only 4-byte alignment, offsets any).
+// A chunk that is not entirely inside the packet buffer is read word by word
+// with the same bounds rule as the unstaged path (a word at an offset below
+// the buffer length is read), and nothing is read for a signature whose
+// fields are out of range (its verdict is false either way).
+constexpr int kStageStride = 33;
+constexpr int kStageWords = 32 * kStageStride;
+
+__device__ __forceinline__ uint4 stage_chunk(const uint8_t* base, uint64_t len, uintptr_t start) {
+    const uintptr_t b0 = reinterpret_cast<uintptr_t>(base);
+    if (start >= b0 && start + 16 <= b0 + len) return __ldg(reinterpret_cast<const uint4*>(start));
+    uint32_t w[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const uintptr_t at = start + 4u * k;
+        w[k] = (at >= b0 && at - b0 < len) ? __ldg(reinterpret_cast<const uint32_t*>(at)) : 0u;
+    }
+    return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+__device__ __forceinline__ void stage_sig_pk(uint32_t words[24], const SigBatch& a, uint32_t* raw, uint32_t lane,
+                                             uint64_t so, uint64_t po, bool ok) {
+    const uintptr_t b0 = reinterpret_cast<uintptr_t>(a.packets);
+    const uintptr_t sa = b0 + so, pa = b0 + po;          // this lane's signature and key
+    const uint32_t c = lane & 7u;
+#pragma unroll 1
+    for (uint32_t r = 0; r < 8; r++) {
+        const uint32_t src = 4u * r + (lane >> 3);
+        const uint64_t s_at = __shfl_sync(0xffffffffu, (unsigned long long)sa, src);
+        const uint64_t p_at = __shfl_sync(0xffffffffu, (unsigned long long)pa, src);
+        const bool s_ok = __shfl_sync(0xffffffffu, ok ? 1u : 0u, src) != 0u;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (s_ok) {
+            const uintptr_t start = c < 5u ? (s_at & ~(uintptr_t)15) + 16u * c : (p_at & ~(uintptr_t)15) + 16u * (c - 5u);
+            v = stage_chunk(a.packets, a.packets_len, start);
+        }
+        raw[(4u * c + 0u) * kStageStride + src] = v.x;
+        raw[(4u * c + 1u) * kStageStride + src] = v.y;
+        raw[(4u * c + 2u) * kStageStride + src] = v.z;
+        raw[(4u * c + 3u) * kStageStride + src] = v.w;
+    }
+    __syncwarp();
+    const uint32_t s_sh = (uint32_t)(sa & 3u) * 8u, s_w = (uint32_t)(sa & 15u) >> 2;
+    const uint32_t p_sh = (uint32_t)(pa & 3u) * 8u, p_w = 20u + ((uint32_t)(pa & 15u) >> 2);
+#pragma unroll
+    for (int k = 0; k < 16; k++)
+        words[k] = __funnelshift_r(raw[(s_w + k) * kStageStride + lane], raw[(s_w + k + 1) * kStageStride + lane], s_sh);
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+        words[16 + k] =
+            __funnelshift_r(raw[(p_w + k) * kStageStride + lane], raw[(p_w + k + 1) * kStageStride + lane], p_sh);
+}
+
+// The one-lane kernel with its signatures and keys staged (above).
+template <int W, int MINB>
+__global__ void __launch_bounds__(VERIFY_THREADS, MINB) ed25519_verify_staged_kernel(SigBatch a) {
+    __shared__ uint32_t sVB[VB_WORDS * VB_ENTRIES];
+    __shared__ uint32_t sRaw[VERIFY_THREADS / 32][kStageWords];
+    for (int k = threadIdx.x; k < VB_WORDS * VB_ENTRIES; k += blockDim.x) sVB[k] = a.tables->vb[k];
+    __syncthreads();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31u;
+    uint64_t so = 0, po = 0;
+    bool ok = false;
+    if (i < a.n) {
+        so = a.signature_offsets[i];
+        po = a.public_key_offsets[i];
+        const uint64_t mo = a.message_start_offsets[i];
+        const uint32_t m = a.message_lens[i];
+        ok = !(so + 64 > a.packets_len || po + 32 > a.packets_len || mo + m > a.packets_len);
+    }
+    uint32_t words[24];
+    stage_sig_pk(words, a, sRaw[threadIdx.x >> 5], lane, so, po, ok);
+    if (i >= a.n) return;
+    a.out[i] = verify_window<W>(a, sVB, i, words) ? 1 : 0;
+}
+
 // Four lanes per signature (verify_quad.cuh): signature t / 4 on lane t % 4.
 // A quad leaves the kernel together (blockDim is a multiple of 4).
 __global__ void __launch_bounds__(VERIFY_THREADS, VERIFY_MIN_BLOCKS) ed25519_verify_quad_kernel(SigBatch a) {
@@ -137,6 +228,7 @@ cudaError_t preload_verify_kernels() {
     return load_kernels(ed25519_verify_kernel<4, VERIFY_MIN_BLOCKS>, ed25519_verify_kernel<4, 4>,
                         ed25519_verify_kernel<5, VERIFY_MIN_BLOCKS>, ed25519_verify_quad_kernel,
                         ed25519_verify_trio_kernel<1>, ed25519_verify_trio_kernel<2>, half_scalars_kernel,
+                        ed25519_verify_staged_kernel<4, VERIFY_MIN_BLOCKS>, ed25519_verify_staged_kernel<4, 4>,
                         check_small_order_kernel);
 }
 
@@ -162,6 +254,16 @@ cudaError_t launch_ed25519_verify_form(const SigBatch& b, cudaStream_t s, int fo
         if (threads > 0xffffffffull) return cudaErrorInvalidValue;
         const uint32_t blocks = (uint32_t)((threads + VERIFY_THREADS - 1) / VERIFY_THREADS);
         ed25519_verify_quad_kernel<<<blocks, VERIFY_THREADS, 0, s>>>(b);
+    } else if (form == kVerifyStaged) {
+        const uint32_t blocks = (b.n + VERIFY_THREADS - 1) / VERIFY_THREADS;
+        int dev = 0, sms = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            return cudaGetLastError();
+        if ((uint64_t)b.n >= 4ull * VERIFY_THREADS * (uint64_t)sms)
+            ed25519_verify_staged_kernel<4, 4><<<blocks, VERIFY_THREADS, 0, s>>>(b);
+        else
+            ed25519_verify_staged_kernel<4, VERIFY_MIN_BLOCKS><<<blocks, VERIFY_THREADS, 0, s>>>(b);
     } else {
         const uint32_t blocks = (b.n + VERIFY_THREADS - 1) / VERIFY_THREADS;
         if (b.window == 5) {
