@@ -153,8 +153,9 @@ struct SvcDevice {           // device memory, zeroed at creation
     uint32_t stop;           // nonzero: warps leave as soon as the FIFO is empty
     uint32_t exiting;        // nonzero: the launch is idle and every warp leaves (reset before a launch)
     uint64_t last_claim_ns;  // %globaltimer of the launch's latest claim (reset before a launch)
+    uint32_t busy_first;     // first-block warps running a chunk (reset before a launch)
     uint32_t warps;          // warps that started (diagnostic)
-    uint32_t pad;
+    uint32_t sm_blocks[256]; // blocks of the launch started on each SM (reset before a launch)
 };
 struct SvcParams {
     SvcDevice* dev;
@@ -167,6 +168,7 @@ struct SvcParams {
     uint64_t* times;         // device view of host memory [2 * max_req]: a completed request's first
                              // claim and completion times (%globaltimer), written before `done`
     uint32_t ring_size;
+    uint32_t first_warps;    // warps of the first block on each SM (one per sub-partition), all SMs
     uint64_t idle_ns;        // the launch leaves (all warps together) after this long without a claim
     const CurveTables* tables;
 };

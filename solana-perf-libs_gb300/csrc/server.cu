@@ -500,6 +500,7 @@ bool svc_create(gb300_server* sv) {
     const char* idle = getenv("GB300_CRYPT_SERVER_IDLE_US");
     V.params.idle_ns = 1000ull * (uint64_t)(idle && atoi(idle) > 0 ? atoi(idle) : 20000);
     V.params.tables = sv->info.tables;
+    V.params.first_warps = 4u * (uint32_t)sv->info.sms;
     if (const char* b = getenv("GB300_CRYPT_SERVER_SVC_BLOCKS")) V.blocks_per_sm = atoi(b) > 0 ? atoi(b) : 2;
     void* fn = nullptr;
     cudaDriverEntryPointQueryResult q;
@@ -567,8 +568,9 @@ void svc_ensure_running(gb300_server* sv) {
     }
     // the launch's exit flag and claim time start from zero (stream order:
     // after the previous launch has left)
-    cudaError_t e = cudaMemsetAsync(&V.d_state->exiting, 0, offsetof(SvcDevice, warps) - offsetof(SvcDevice, exiting),
-                                    V.run);
+    cudaError_t e = cudaMemsetAsync(&V.d_state->exiting, 0,
+                                    offsetof(SvcDevice, warps) - offsetof(SvcDevice, exiting), V.run);
+    if (e == cudaSuccess) e = cudaMemsetAsync(V.d_state->sm_blocks, 0, sizeof(V.d_state->sm_blocks), V.run);
     if (e == cudaSuccess) e = launch_sig_service(V.params, V.blocks_per_sm, sv->info.sms, V.run);
     if (e == cudaSuccess) e = cudaEventRecord(V.run_done, V.run);
     if (e != cudaSuccess) {

@@ -108,7 +108,8 @@ __device__ __forceinline__ S ld_volatile_struct(const S* p) {
 // GB300 with ncu, the four-lane verify then issued twice its instructions
 // with ~20 active threads and 2.6 branch-resolution stalls per issue, and
 // eight signatures took 3.0 ms against 0.46 ms in a plain launch.
-__device__ __forceinline__ bool claim_chunk(const SvcParams& p, uint32_t lane, uint32_t& c, uint64_t t_start) {
+__device__ __forceinline__ bool claim_chunk(const SvcParams& p, uint32_t lane, uint32_t& c, uint64_t t_start,
+                                            bool first) {
     uint32_t sleep_ns = 256;
     for (;;) {
         uint32_t r = 3, got = 0;      // 0 leave, 1 claimed, 2 lost a race (look again), 3 empty
@@ -118,7 +119,12 @@ __device__ __forceinline__ bool claim_chunk(const SvcParams& p, uint32_t lane, u
             } else {
                 const uint32_t t = ld_relaxed_gpu(&p.dev->tail);
                 const uint32_t h = ld_relaxed_gpu(&p.dev->head);
-                if ((int32_t)(t - h) > 0) {
+                // a warp of an SM's second block takes a chunk only when the
+                // waiting chunks outnumber the idle first-block warps
+                const int32_t waiting = (int32_t)(t - h);
+                const bool mine = waiting > 0 &&
+                                  (first || waiting > (int32_t)(p.first_warps - ld_relaxed_gpu(&p.dev->busy_first)));
+                if (mine) {
                     if (atomicCAS(&p.dev->head, h, h + 1u) == h) {
                         r = 1;
                         got = h;
@@ -127,7 +133,7 @@ __device__ __forceinline__ bool claim_chunk(const SvcParams& p, uint32_t lane, u
                     } else {
                         r = 2;
                     }
-                } else {
+                } else if (waiting <= 0) {
                     const uint64_t last = ld_relaxed_gpu64(&p.dev->last_claim_ns);
                     const uint64_t since = last > t_start ? last : t_start;
                     const uint64_t now = global_ns();
@@ -159,7 +165,14 @@ __device__ __forceinline__ bool claim_chunk(const SvcParams& p, uint32_t lane, u
 template <int T, int W>
 __global__ void __maxnreg__(216) sig_service_kernel(SvcParams p) {
     __shared__ uint32_t sVB[VB_WORDS * VB_ENTRIES];
+    __shared__ uint32_t s_rank;
     extern __shared__ uint4 s_comb4[];
+    if (threadIdx.x == 0) {
+        // this block's rank among the launch's blocks on its SM
+        uint32_t smid;
+        asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+        s_rank = atomicAdd(&p.dev->sm_blocks[smid & 255u], 1u);
+    }
     for (int k = threadIdx.x; k < VB_WORDS * VB_ENTRIES; k += blockDim.x) sVB[k] = p.tables->vb[k];
     {
         const uint4* g = reinterpret_cast<const uint4*>(&p.tables->comb[0][0]);
@@ -168,11 +181,18 @@ __global__ void __maxnreg__(216) sig_service_kernel(SvcParams p) {
     __syncthreads();
     const ge_niels* comb = reinterpret_cast<const ge_niels*>(s_comb4);
     const uint32_t lane = threadIdx.x & 31u;
+    // The first block on each SM has one warp on each sub-partition; its
+    // warps take chunks first, so that a few chunks spread over the SMs'
+    // sub-partitions instead of doubling up on some while others idle (a
+    // verify chain is latency-bound: a second warp on the same
+    // sub-partition slows both).
+    const bool first = s_rank == 0;
     const uint64_t t_start = global_ns();
     if (lane == 0) atomicAdd(&p.dev->warps, 1u);
     for (;;) {
         uint32_t c = 0;
-        if (!claim_chunk(p, lane, c, t_start)) break;
+        if (!claim_chunk(p, lane, c, t_start, first)) break;
+        if (first && lane == 0) atomicAdd(&p.dev->busy_first, 1u);
         // every lane synchronises with the publication of chunk c (the
         // stream write of tail after the input copies): its later loads of
         // the descriptors (host memory) and inputs (device memory) see them
@@ -198,6 +218,7 @@ __global__ void __maxnreg__(216) sig_service_kernel(SvcParams p) {
                 b.out[i] = verify_window<W>(b, sVB, i) ? 1 : 0;
             }
         }
+        if (first && lane == 0) atomicSub(&p.dev->busy_first, 1u);
         // results (host memory) before the count; the completing warp
         // resets the slot's counter, then publishes the completion word
         __threadfence_system();
