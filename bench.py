@@ -1339,8 +1339,8 @@ def run_case(case: str):
                 (sp.message_lens, sp.public_key_offsets, sp.signature_offsets, sp.message_start_offsets)]
         out = torch.zeros(sp.total_signatures, dtype=torch.uint8, device="cuda")
         pk = dev(sp.concatenated())
-        for _ in range(3):   # the one-lane kernel (9,728 would pick the four-lane form by size)
-            lib.verify_device_form(pk, *arrs, out, lib.VERIFY_SINGLE_W4, stream.cuda_stream)
+        for _ in range(3):   # the one-lane kernel, tuned form (9,728 would pick the four-lane form by size)
+            lib.verify_device_form(pk, *arrs, out, lib.VERIFY_SINGLE, stream.cuda_stream)
     elif case == "ragged-batch-small":
         # ragged verify jobs + 128-packet sign jobs in one persistent launch, device-resident
         rs = workloads.ragged_sigs(lib.create_keypairs, lib.sign_many, n_batches=12, seed=3)
@@ -1370,8 +1370,8 @@ def run_case(case: str):
                 (sp.message_lens, sp.public_key_offsets, sp.signature_offsets, sp.message_start_offsets)]
         out = torch.zeros(sp.total_signatures, dtype=torch.uint8, device="cuda")
         pk = dev(sp.concatenated())
-        for _ in range(2):
-            lib.verify_device_form(pk, *arrs, out, lib.VERIFY_SINGLE_W4, stream.cuda_stream)
+        for _ in range(2):   # the one-lane kernel, tuned form (the bench's GPU-filling batch)
+            lib.verify_device_form(pk, *arrs, out, lib.VERIFY_SINGLE, stream.cuda_stream)
     elif case == "sign-small":
         bench_sign_device(lib, torch, 152 * 64, reps=2)
     elif case in ("verify-1024-single", "verify-1024-quad", "verify-1024-trio"):

@@ -45,7 +45,8 @@ int gb300_poh_verify_batch_shape(uint8_t* hashes, const uint64_t* num_hashes, ui
  * window, 3 the same with a 5-bit window, 4 three warps per eight
  * signatures with half-size scalars, 5 one thread per signature (4-bit
  * window) with the signatures and keys staged through shared memory by
- * coalesced 16-byte loads.  Same verdicts in every form; used to test and
+ * coalesced 16-byte loads, 6 one thread per signature with half-size
+ * scalars (form 0 is the autotuner's choice of 6 or 2).  Same verdicts in every form; used to test and
  * time each.  Returns a cudaError_t. */
 int gb300_ed25519_verify_device_form(const uint8_t* packets, uint64_t packets_len, const uint32_t* message_lens,
                                      const uint32_t* public_key_offsets, const uint32_t* signature_offsets,

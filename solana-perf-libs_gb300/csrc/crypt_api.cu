@@ -94,10 +94,10 @@ struct Queue {
 struct Tuning {
     int sig_threads = 128;        // threads per block of the persistent sign/verify kernel
     int sig_blocks_per_sm = 0;    // 0 = as many as fit
-    int verify_window = 4;        // signed window width of h in the one-lane verify (4 or 5)
+    int verify_window = 0;        // one-lane verify: 0 half-size scalars, or the window width of h (4 or 5)
     int poh_warps_per_smsp = 1;   // resident warps of the persistent PoH kernel per SM sub-partition
     int poh_form = kPohSingle;    // PohBatchForm of ragged PoH batches
-    double sig_ms[2][3] = {{0, 0, 0}, {0, 0, 0}};  // calibration: window 4 / 5 x 64 / 128 / 256 threads
+    double sig_ms[2][3] = {{0, 0, 0}, {0, 0, 0}};  // calibration: half-size scalars / window 4 x 64 / 128 / 256 threads
     double poh_ms[4] = {0, 0, 0, 0};  // calibration: single and paired forms, 1 and 2 warps per sub-partition
     int calib_sigs = 0, calib_chains = 0;
 };
@@ -340,13 +340,14 @@ void tune_device(Device& D) {
         w.sign_base = (nv + 31u) / 32u * 32u;
         w.total_chunks = (w.sign_base + ns + 31u) / 32u;
         w.next = dq;
-        // the default (window 4, 128 threads) is timed first; another shape
-        // replaces it only when it is more than 2 % faster, so timing noise
-        // does not move the choice from run to run
+        // the default (half-size scalars, 128 threads) is timed first;
+        // another shape replaces it only when it is more than 2 % faster, so
+        // timing noise does not move the choice from run to run
         const int cand[3] = {128, 64, 256};
+        const int windows[2] = {0, 4};
         double best = 1e30;
         for (int wi = 0; wi < 2; wi++) {
-            w.v.window = 4 + wi;
+            w.v.window = windows[wi];
             for (int c = 0; c < 3; c++) {
                 cudaError_t err = cudaSuccess;
                 launch_sig_batch(w, cand[c], 0, sms, s);   // warm
@@ -360,7 +361,7 @@ void tune_device(Device& D) {
                 if (best == 1e30 || ms < 0.98 * best) {
                     best = ms;
                     T.sig_threads = cand[c];
-                    T.verify_window = 4 + wi;
+                    T.verify_window = windows[wi];
                 }
             }
         }
@@ -408,7 +409,10 @@ void tune_device(Device& D) {
     cudaStreamDestroy(s);
     T.sig_threads = env_int("GB300_CRYPT_SIG_THREADS", T.sig_threads);
     T.sig_blocks_per_sm = env_int("GB300_CRYPT_SIG_BLOCKS", T.sig_blocks_per_sm);
-    T.verify_window = env_int("GB300_CRYPT_VERIFY_WINDOW", T.verify_window) == 5 ? 5 : 4;
+    {
+        const int wv = env_int("GB300_CRYPT_VERIFY_WINDOW", T.verify_window);
+        T.verify_window = (wv == 4 || wv == 5) ? wv : 0;
+    }
     T.poh_warps_per_smsp = env_int("GB300_CRYPT_POH_WARPS_PER_SMSP", T.poh_warps_per_smsp);
     T.poh_form = env_int("GB300_CRYPT_POH_PAIRED", T.poh_form == kPohPair) ? kPohPair : kPohSingle;
     LOG("tuned gpu %d: sig threads %d window %d (ms %.3f %.3f %.3f / %.3f %.3f %.3f), poh warps/smsp %d %s "
@@ -440,7 +444,7 @@ const Tuning& tuning_for(Device& D) {
 // The tuned verify window when the device has been tuned, else 4: the
 // one-call device entry points do not start the tuner (it allocates and
 // synchronises, which a caller capturing a graph cannot allow).
-int verify_window_if_tuned(Device& D) { return D.tuned_done.load() ? D.tune.verify_window : 4; }
+int verify_window_if_tuned(Device& D) { return D.tuned_done.load() ? D.tune.verify_window : 0; }
 
 // Stages one signature batch, runs verify or sign on it and copies the
 // results into `out` (n bytes, or 64n bytes for signing).
@@ -769,13 +773,13 @@ int gb300_ed25519_verify_device_form(const uint8_t* packets, uint64_t packets_le
                                      const uint32_t* message_start_offsets, uint32_t num, uint8_t* out, int form,
                                      void* stream) {
     if (num == 0) return 0;
-    if (form < 0 || form > 5) return (int)cudaErrorInvalidValue;
+    if (form < 0 || form > 6) return (int)cudaErrorInvalidValue;
     Device* D = current_device();
     if (!D) return (int)cudaErrorNoDevice;
     if (reinterpret_cast<uintptr_t>(packets) & 3u) return (int)cudaErrorMisalignedAddress;
     SigBatch b{packets, packets_len, message_lens, public_key_offsets, signature_offsets,
                message_start_offsets, num, out, D->tables};
-    b.window = form == 2 ? 4 : form == 3 ? 5 : verify_window_if_tuned(*D);
+    b.window = form == 2 ? 4 : form == 3 ? 5 : form == 6 ? 0 : verify_window_if_tuned(*D);
     return (int)launch_ed25519_verify_form(b, static_cast<cudaStream_t>(stream),
                                            form == 1 ? kVerifyQuad : form == 4 ? kVerifyTrio : form == 5 ? kVerifyStaged : kVerifySingle);
 }
@@ -825,8 +829,8 @@ int gb300_crypt_tuning(char* buf, size_t len) {
     int n = snprintf(buf, len,
                      "{\"device\": %d, \"sms\": %d, \"sig_threads\": %d, \"sig_blocks_per_sm\": %d, "
                      "\"verify_window\": %d, "
-                     "\"sig_calibration_ms\": {\"w4\": {\"64\": %.4f, \"128\": %.4f, \"256\": %.4f}, "
-                     "\"w5\": {\"64\": %.4f, \"128\": %.4f, \"256\": %.4f}}, "
+                     "\"sig_calibration_ms\": {\"half\": {\"64\": %.4f, \"128\": %.4f, \"256\": %.4f}, "
+                     "\"w4\": {\"64\": %.4f, \"128\": %.4f, \"256\": %.4f}}, "
                      "\"sig_calibration_items\": %d, \"poh_warps_per_smsp\": %d, \"poh_paired\": %d, "
                      "\"poh_calibration_ms\": {\"single_1\": %.4f, \"single_2\": %.4f, \"paired_1\": %.4f, "
                      "\"paired_2\": %.4f}, \"poh_calibration_chains\": %d}",

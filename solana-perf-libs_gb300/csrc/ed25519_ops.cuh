@@ -337,11 +337,17 @@ __device__ bool verify_one_w(const SigBatch& a, const uint32_t* sVB, uint32_t i,
     return diff == 0;
 }
 
-// verdict of signature i with window width W (4: verify_one)
+#include "verify_half.cuh"
+
+// Verdict of signature i with window width W of h (4: verify_one, 5:
+// verify_one_w<5>), or W = 0: half-size scalars (verify_half.cuh), which
+// votes over the warp, so every lane of the warp calls (lanes without a
+// signature of their own pass one that exists and drop the verdict).
 template <int W>
 __device__ __forceinline__ bool verify_window(const SigBatch& a, const uint32_t* sVB, uint32_t i,
                                               const uint32_t* staged = nullptr) {
-    if constexpr (W == 4) return verify_one(a, sVB, i, staged);
+    if constexpr (W == 0) return verify_half(a, i, staged);
+    else if constexpr (W == 4) return verify_one(a, sVB, i, staged);
     else return verify_one_w<W>(a, sVB, i, staged);
 }
 

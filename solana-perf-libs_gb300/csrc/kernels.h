@@ -20,7 +20,8 @@ struct SigBatch {
     uint32_t n;
     uint8_t* out;                 // verify: n verdict bytes; sign: n*64 bytes
     const CurveTables* tables;
-    int window = 4;               // verify: signed window width of h (4 or 5; the autotuner's choice)
+    int window = 0;               // verify, one lane per signature: signed window width of h (4 or 5), or 0
+                                  // for half-size scalars (the autotuner's choice)
 };
 
 // Kernels are loaded on the current device when these run, rather than at

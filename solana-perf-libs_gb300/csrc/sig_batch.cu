@@ -71,8 +71,12 @@ __global__ void __launch_bounds__(T, MINB) sig_persistent_kernel(SigWork w) {
                 const bool ok = verify_quad(w.v, sVB, i < vn ? i : vn - 1u, lane & 3u);
                 if (i < vn && (lane & 3u) == 0) w.v.out[i] = ok ? 1 : 0;
             } else {
+                // every lane runs an item (past the end: the last one
+                // again, result dropped): the half-size-scalar form votes
+                // over the warp
                 const uint32_t i = c * 32u + lane;
-                if (i < vn) w.v.out[i] = verify_window<W>(w.v, sVB, i) ? 1 : 0;
+                const bool ok = verify_window<W>(w.v, sVB, i < vn ? i : vn - 1u);
+                if (i < vn) w.v.out[i] = ok ? 1 : 0;
             }
         } else {
             const uint32_t i = (c - vchunks) * 32u + lane;
@@ -124,10 +128,10 @@ cudaError_t launch_t(const SigWork& w, int blocks_per_sm, int sms, cudaStream_t 
 }  // namespace
 
 cudaError_t preload_sig_batch_kernels() {
-    return load_kernels(sig_persistent_kernel<64, 4, 1>, sig_persistent_kernel<64, 5, 1>,
-                        sig_persistent_kernel<128, 4, 1>, sig_persistent_kernel<128, 5, 1>,
-                        sig_persistent_kernel<128, 4, 3>, sig_persistent_kernel<256, 4, 1>,
-                        sig_persistent_kernel<256, 5, 1>);
+    return load_kernels(sig_persistent_kernel<64, 4, 1>, sig_persistent_kernel<64, 0, 1>,
+                        sig_persistent_kernel<128, 4, 1>, sig_persistent_kernel<128, 0, 1>,
+                        sig_persistent_kernel<128, 4, 3>, sig_persistent_kernel<128, 0, 3>,
+                        sig_persistent_kernel<256, 4, 1>, sig_persistent_kernel<256, 0, 1>);
 }
 
 // Verify signatures four lanes each while the batch leaves the GPU idle
@@ -142,24 +146,24 @@ cudaError_t launch_sig_batch(const SigWork& w_in, int threads, int blocks_per_sm
                (form == kVerifyQuad || (form != kVerifySingle && (uint64_t)w.v.n <= 64ull * (uint64_t)sms));
     cudaError_t e = cudaMemsetAsync(w.next, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
-    const bool w5 = w.v.window == 5;
+    const bool half = w.v.window == 0;         // else window 4 (5 is not built for this kernel)
     // a launch with chunks for 3 blocks of 128 threads on every SM runs the
     // build capped at 3 blocks per SM (1 minimum otherwise).  Not a count_dev
     // launch: its size is a capacity, ~10x the signatures of a packet batch
     // (16,384 packets: 2.34 ms in the capped build against 1.66 ms).
     const uint64_t warps = (uint64_t)verify_chunks(w, w.v.n, w.v_quad) + sign_chunks(w);
-    const bool full = threads != 64 && threads != 256 && !w5 && blocks_per_sm < 1 && !w.count_dev &&
+    const bool full = threads != 64 && threads != 256 && blocks_per_sm < 1 && !w.count_dev &&
                       warps >= 12ull * (uint64_t)sms;
     // a count_dev launch sized above the four-lane limit still takes the
     // four-lane form when its device count turns out small
     w.v_quad_max = 0;
     if (w.count_dev && !w.v_quad && form != kVerifySingle) w.v_quad_max = (uint32_t)(64u * (uint32_t)sms);
     switch (threads) {
-        case 64: return w5 ? launch_t<64, 5, 1>(w, blocks_per_sm, sms, s) : launch_t<64, 4, 1>(w, blocks_per_sm, sms, s);
+        case 64: return half ? launch_t<64, 0, 1>(w, blocks_per_sm, sms, s) : launch_t<64, 4, 1>(w, blocks_per_sm, sms, s);
         case 256:
-            return w5 ? launch_t<256, 5, 1>(w, blocks_per_sm, sms, s) : launch_t<256, 4, 1>(w, blocks_per_sm, sms, s);
+            return half ? launch_t<256, 0, 1>(w, blocks_per_sm, sms, s) : launch_t<256, 4, 1>(w, blocks_per_sm, sms, s);
         default:
-            if (full) return launch_t<128, 4, 3>(w, blocks_per_sm, sms, s);
-            return w5 ? launch_t<128, 5, 1>(w, blocks_per_sm, sms, s) : launch_t<128, 4, 1>(w, blocks_per_sm, sms, s);
+            if (full) return half ? launch_t<128, 0, 3>(w, blocks_per_sm, sms, s) : launch_t<128, 4, 3>(w, blocks_per_sm, sms, s);
+            return half ? launch_t<128, 0, 1>(w, blocks_per_sm, sms, s) : launch_t<128, 4, 1>(w, blocks_per_sm, sms, s);
     }
 }

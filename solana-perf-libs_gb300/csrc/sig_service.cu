@@ -213,10 +213,12 @@ __global__ void __maxnreg__(216) sig_service_kernel(SvcParams p) {
         } else if (ch.mode == kSvcSign) {
             if (lane < ch.count) sign_one_tab(b, ch.first + lane, comb);
         } else {
-            if (lane < ch.count) {
-                const uint32_t i = ch.first + lane;
-                b.out[i] = verify_window<W>(b, sVB, i) ? 1 : 0;
-            }
+            // every lane runs an item (past the end: the chunk's last
+            // again, result dropped): the half-size-scalar form votes over
+            // the warp
+            const uint32_t i = ch.first + (lane < ch.count ? lane : ch.count - 1u);
+            const bool ok = verify_window<W>(b, sVB, i);
+            if (lane < ch.count) b.out[i] = ok ? 1 : 0;
         }
         if (first && lane == 0) atomicSub(&p.dev->busy_first, 1u);
         // results (host memory) before the count; the completing warp
@@ -238,7 +240,8 @@ __global__ void __maxnreg__(216) sig_service_kernel(SvcParams p) {
     }
 }
 
-#define SVC_KERNEL sig_service_kernel<kSvcThreads, 4>
+// one-lane chunks with half-size scalars (verify_half.cuh)
+#define SVC_KERNEL sig_service_kernel<kSvcThreads, 0>
 
 // %globaltimer now, for relating the kernel's times to the host clock.
 __global__ void svc_clock_kernel(uint64_t* out) { *reinterpret_cast<volatile uint64_t*>(out) = global_ns(); }

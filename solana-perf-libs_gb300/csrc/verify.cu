@@ -45,20 +45,27 @@ namespace {
 #include "ed25519_ops.cuh"
 #include "verify_quad.cuh"
 #include "verify_trio.cuh"
+#include "verify_half.cuh"
 
 // MINB: blocks per SM the register allocation must allow.  1 lets the
 // compiler keep everything in registers (254; 2 blocks of 128 fit); 4 caps
 // it at 128 registers, with some spills, for batches large enough to fill
 // 4 blocks per SM, where the extra warps hide more latency (measured at
 // 116,736 signatures: 4.27 ms against 4.57; at 32,768 it is 4 % slower).
+// W: the window width of h (4 or 5), or 0 for half-size scalars
+// (verify_half.cuh).  Whole warps run: lanes past the batch repeat its last
+// signature and drop the verdict.
 template <int W, int MINB>
 __global__ void __launch_bounds__(VERIFY_THREADS, MINB) ed25519_verify_kernel(SigBatch a) {
     __shared__ uint32_t sVB[VB_WORDS * VB_ENTRIES];
-    for (int k = threadIdx.x; k < VB_WORDS * VB_ENTRIES; k += blockDim.x) sVB[k] = a.tables->vb[k];
-    __syncthreads();
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n) return;
-    a.out[i] = verify_window<W>(a, sVB, i) ? 1 : 0;
+    if (W != 0) {
+        for (int k = threadIdx.x; k < VB_WORDS * VB_ENTRIES; k += blockDim.x) sVB[k] = a.tables->vb[k];
+        __syncthreads();
+    }
+    const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t i = gi < a.n ? gi : a.n - 1u;
+    const bool ok = verify_window<W>(a, sVB, i);
+    if (gi < a.n) a.out[gi] = ok ? 1 : 0;
 }
 
 // Packet staging for the one-lane kernel: each warp brings the 64-byte
@@ -229,6 +236,7 @@ cudaError_t preload_verify_kernels() {
                         ed25519_verify_kernel<5, VERIFY_MIN_BLOCKS>, ed25519_verify_quad_kernel,
                         ed25519_verify_trio_kernel<1>, ed25519_verify_trio_kernel<2>, half_scalars_kernel,
                         ed25519_verify_staged_kernel<4, VERIFY_MIN_BLOCKS>, ed25519_verify_staged_kernel<4, 4>,
+                        ed25519_verify_kernel<0, VERIFY_MIN_BLOCKS>, ed25519_verify_kernel<0, 4>,
                         check_small_order_kernel);
 }
 
@@ -273,10 +281,15 @@ cudaError_t launch_ed25519_verify_form(const SigBatch& b, cudaStream_t s, int fo
             if (cudaGetDevice(&dev) != cudaSuccess ||
                 cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
                 return cudaGetLastError();
-            if ((uint64_t)b.n >= 4ull * VERIFY_THREADS * (uint64_t)sms)
+            const bool big = (uint64_t)b.n >= 4ull * VERIFY_THREADS * (uint64_t)sms;
+            if (b.window == 0) {
+                if (big) ed25519_verify_kernel<0, 4><<<blocks, VERIFY_THREADS, 0, s>>>(b);
+                else ed25519_verify_kernel<0, VERIFY_MIN_BLOCKS><<<blocks, VERIFY_THREADS, 0, s>>>(b);
+            } else if (big) {
                 ed25519_verify_kernel<4, 4><<<blocks, VERIFY_THREADS, 0, s>>>(b);
-            else
+            } else {
                 ed25519_verify_kernel<4, VERIFY_MIN_BLOCKS><<<blocks, VERIFY_THREADS, 0, s>>>(b);
+            }
         }
     }
     return cudaGetLastError();

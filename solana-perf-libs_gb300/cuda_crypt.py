@@ -438,7 +438,7 @@ class CudaCrypt:
         if rc != 0:
             raise RuntimeError(f"gb300_ed25519_verify_device: cudaError {rc}")
 
-    VERIFY_SINGLE, VERIFY_QUAD, VERIFY_SINGLE_W4, VERIFY_SINGLE_W5, VERIFY_TRIO, VERIFY_STAGED = 0, 1, 2, 3, 4, 5
+    VERIFY_SINGLE, VERIFY_QUAD, VERIFY_SINGLE_W4, VERIFY_SINGLE_W5, VERIFY_TRIO, VERIFY_STAGED, VERIFY_HALF = 0, 1, 2, 3, 4, 5, 6
 
     def verify_device_form(self, packets, message_lens, public_key_offsets, signature_offsets,
                            message_start_offsets, out, form, stream=0) -> None:

@@ -121,8 +121,8 @@ def test_sig_batch_device(lib, oracle):
 def test_tuning_report(lib):
     t = lib.tuning()
     assert t["sig_threads"] in (64, 128, 256)
-    assert t["verify_window"] in (4, 5)
-    assert set(t["sig_calibration_ms"]) == {"w4", "w5"}
+    assert t["verify_window"] in (0, 4)                 # half-size scalars or the 4-bit window
+    assert set(t["sig_calibration_ms"]) == {"half", "w4"}
     assert t["poh_warps_per_smsp"] in (1, 2)
     assert t["poh_paired"] in (0, 1)
     assert t["sms"] > 0
@@ -211,3 +211,33 @@ def test_sig_batch_both_verify_modes(lib, oracle):
         assert np.array_equal(got, exp), n
         assert np.array_equal(lib.verify_many(sp), exp), n
         assert np.array_equal(got.astype(bool), ~corrupted)
+
+
+def test_sig_batch_window4_form(oracle, tmp_path):
+    """The 4-bit-window one-lane form in the batched kernel (the autotuner
+    normally keeps half-size scalars; GB300_CRYPT_VERIFY_WINDOW=4 forces the
+    window, read once per process, so a child process runs it) gives the
+    oracle's verdicts."""
+    import os
+    import subprocess
+    import sys
+    rs = _ragged(oracle, 71, n_batches=3, cap=300)
+    script = f"""
+import sys, numpy as np
+sys.path[:0] = {[os.path.dirname(os.path.abspath(__file__)), os.path.dirname(os.path.dirname(os.path.abspath(__file__))), os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "solana-perf-libs_gb300")]!r}
+import cuda_crypt, workloads
+from cuda_crypt import JOB_VERIFY
+from oracle.oracle import get_oracle
+o = get_oracle()
+rs = workloads.ragged_sigs(o.create_keypairs, o.sign_packets, n_batches=3, total_packet_cap=300, seed=71)
+lib = cuda_crypt.get_lib()
+assert lib.init()
+assert lib.tuning()["verify_window"] == 4
+outs = lib.ed25519_batch([(sp, JOB_VERIFY) for sp in rs.verify])
+np.save({str(tmp_path / "v.npy")!r}, np.concatenate(outs))
+"""
+    env = dict(os.environ, GB300_CRYPT_VERIFY_WINDOW="4")
+    subprocess.run([sys.executable, "-c", script], env=env, check=True, timeout=600)
+    got = np.load(tmp_path / "v.npy")
+    exp = np.concatenate([oracle.verify_packets(sp, nthreads()) for sp in rs.verify])
+    assert np.array_equal(got, exp)

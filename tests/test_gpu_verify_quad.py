@@ -33,7 +33,7 @@ def run_form(lib, sp, form):
 
 def ALL_FORMS(lib):
     return (lib.VERIFY_SINGLE, lib.VERIFY_QUAD, lib.VERIFY_SINGLE_W4, lib.VERIFY_SINGLE_W5, lib.VERIFY_TRIO,
-            lib.VERIFY_STAGED)
+            lib.VERIFY_STAGED, lib.VERIFY_HALF)
 
 
 def both_forms(lib, oracle, sp):
@@ -167,7 +167,7 @@ def test_verify_form_rejects_bad_form(lib):
     z = torch.zeros(4, dtype=torch.int32, device="cuda")
     out = torch.zeros(4, dtype=torch.uint8, device="cuda")
     with pytest.raises(RuntimeError):
-        lib.verify_device_form(torch.zeros(256, dtype=torch.uint8, device="cuda"), z, z, z, z, out, 6)
+        lib.verify_device_form(torch.zeros(256, dtype=torch.uint8, device="cuda"), z, z, z, z, out, 7)
 
 
 def test_half_scalars_chosen_h(lib):
