@@ -241,3 +241,20 @@ np.save({str(tmp_path / "v.npy")!r}, np.concatenate(outs))
     got = np.load(tmp_path / "v.npy")
     exp = np.concatenate([oracle.verify_packets(sp, nthreads()) for sp in rs.verify])
     assert np.array_equal(got, exp)
+
+
+def test_sig_batch_mixed_order_keys(lib, oracle):
+    """Keys and nonces with small-order components in the batched kernel:
+    four lanes (a launch within the four-lane limit) and one lane with
+    half-size scalars (the same items beside enough others to pass it)."""
+    from test_gpu_verify import pack_items
+    from test_gpu_verify_quad import _valid_items, mixed_order_items
+    sms = lib.tuning()["sms"]
+    mixed = mixed_order_items(n=96, seed=77)
+    filler, _ = _valid_items(oracle, 64 * sms + 200, 78, msg_len=32)
+    small = pack_items(mixed, gap_seed=12)
+    big = pack_items(mixed + filler, gap_seed=13)
+    out = lib.ed25519_batch([(small, JOB_VERIFY)])[0]
+    assert np.array_equal(out, oracle.verify_packets(small, nthreads()))
+    out = lib.ed25519_batch([(big, JOB_VERIFY)])[0]
+    assert np.array_equal(out, oracle.verify_packets(big, nthreads()))

@@ -262,3 +262,27 @@ def test_service_job_too_large_for_its_rings_takes_a_slot(lib, oracle):
         assert st["service"]["to_slots"] == 1 and st["service"]["served"] == 2
     finally:
         srv.close()
+
+
+def test_service_mixed_order_keys(lib, oracle):
+    """Keys and nonces with small-order components through the service, in
+    four-lane chunks (a small job) and in one-lane chunks with half-size
+    scalars (the same items at the front of a job above the four-lane
+    limit): the oracle's verdicts."""
+    from test_gpu_verify import pack_items
+    from test_gpu_verify_quad import _valid_items, mixed_order_items
+    sms = lib.tuning()["sms"]
+    mixed = mixed_order_items(n=96, seed=75)
+    filler, _ = _valid_items(oracle, 64 * sms + 200, 76, msg_len=32)
+    small = pack_items(mixed, gap_seed=10)
+    big = pack_items(mixed + filler, gap_seed=11)
+    exp_small = oracle.verify_packets(small, nthreads())
+    exp_big = oracle.verify_packets(big, nthreads())
+    assert 0 < int(exp_small.sum()) < len(mixed)
+    srv = Server(lib)
+    try:
+        for sp, exp in ((small, exp_small), (big, exp_big)):
+            t, out = srv.submit_sigs(sp, JOB_VERIFY)
+            assert srv.wait(t, 60000) == 1 and np.array_equal(out, exp)
+    finally:
+        srv.close()

@@ -126,21 +126,20 @@ def test_quad_message_lengths_and_random(lib, oracle):
     both_forms(lib, oracle, pack_items(cases, gap_seed=7))
 
 
-def test_mixed_order_keys_and_nonces(lib, oracle):
-    """A = aB + T and R = rB + T' with small-order T, T' (every order 1..8),
-    signed with the discrete logs: S = r + h a mod L.  The reference's
-    cofactorless check accepts exactly when [h]T = -T' (e.g. T' neutral and
-    8 | h for T of order 8), so both verdicts occur; the half-size-scalar
-    form must agree with the oracle on every one (its modulus 8L keeps the
-    small-order part of [h]A exact)."""
+def mixed_order_items(n=160, seed=57):
+    """(signature, message, public key) items with A = aB + T and
+    R = rB + T' for small-order T, T' (every order 1..8), signed with the
+    discrete logs: S = r + h a mod L.  The reference's cofactorless check
+    accepts exactly when [h]T = -T' (e.g. T' neutral and 8 | h for T of
+    order 8), so both verdicts occur."""
     import hashlib
     import ed25519_math as E
     by = 4 * pow(5, E.P - 2, E.P) % E.P
     B = (E.recover_x(by, 0), by)
     tors = E.torsion_points()
-    rng = np.random.default_rng(57)
+    rng = np.random.default_rng(seed)
     cases = []
-    for k in range(160):
+    for k in range(n):
         a = int.from_bytes(rng.bytes(32), "little") % E.L
         r = int.from_bytes(rng.bytes(32), "little") % E.L
         ta = tors[k % len(tors)]
@@ -151,6 +150,14 @@ def test_mixed_order_keys_and_nonces(lib, oracle):
         h = int.from_bytes(hashlib.sha512(R + A + msg).digest(), "little") % E.L
         S = (r + h * a) % E.L
         cases.append((R + S.to_bytes(32, "little"), msg, A))
+    return cases
+
+
+def test_mixed_order_keys_and_nonces(lib, oracle):
+    """Every form agrees with the oracle on keys and nonces with small-order
+    components (the half-size-scalar forms: their modulus 8L keeps the
+    small-order part of [h]A exact)."""
+    cases = mixed_order_items()
     exp = both_forms(lib, oracle, pack_items(cases, gap_seed=9))
     assert 0 < int(exp.sum()) < len(cases)
 
