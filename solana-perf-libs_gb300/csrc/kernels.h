@@ -154,7 +154,7 @@ struct SvcDevice {           // device memory, zeroed at creation
     uint32_t stop;           // nonzero: warps leave as soon as the FIFO is empty
     uint32_t exiting;        // nonzero: the launch is idle and every warp leaves (reset before a launch)
     uint64_t last_claim_ns;  // %globaltimer of the launch's latest claim (reset before a launch)
-    uint32_t busy_first;     // first-block warps running a chunk (reset before a launch)
+    uint32_t busy_first;     // preferred warps running a chunk (reset before a launch)
     uint32_t warps;          // warps that started (diagnostic)
     uint32_t sm_blocks[256]; // blocks of the launch started on each SM (reset before a launch)
 };
@@ -170,6 +170,8 @@ struct SvcParams {
                              // claim and completion times (%globaltimer), written before `done`
     uint32_t ring_size;
     uint32_t first_warps;    // warps of the first block on each SM (one per sub-partition), all SMs
+    const uint32_t* poh_slots;       // PoH round warps per SM sub-partition (poh_round_warp_map)
+    const uint32_t* poh_busy_slots;  // sub-partitions with a PoH round warp
     uint64_t idle_ns;        // the launch leaves (all warps together) after this long without a claim
     const CurveTables* tables;
 };
@@ -180,6 +182,13 @@ struct SvcParams {
 // fit, and L1 keeps ~92 KB for the verify path's per-thread point tables
 // (local memory).
 constexpr int kServeCarveoutPercent = 72;
+
+// SMs covered by the PoH placement map (poh_batch.cu); SM indices wrap.
+constexpr uint32_t kMaxServeSms = 256;
+// Device addresses of the PoH round warps' placement map on the current
+// device: round warps per SM sub-partition (kMaxServeSms x 4) and the count
+// of sub-partitions with at least one.
+cudaError_t poh_round_warp_map(const uint32_t** per_slot, const uint32_t** busy_slots);
 
 // Blocks of the service kernel that fit on one SM (sets its shared-memory
 // attributes on the current device first).

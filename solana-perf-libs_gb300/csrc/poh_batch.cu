@@ -140,11 +140,35 @@ static __device__ __noinline__ HashWords single_run(HashWords in, uint64_t r, ui
     return out;
 }
 
+// Where the persistent kernels' round warps run: per SM sub-partition (SM
+// index x 4 + the warp slot's sub-partition), the round warps there now,
+// and how many sub-partitions have at least one.  The served loop's
+// signature service reads them (poh_round_warp_map) to prefer
+// sub-partitions without one: a verify chain beside an ALU-bound round warp
+// gets about half of the sub-partition's issue slots.  Diagnostic-grade
+// placement (%warpid is the warp's slot when read); only a preference
+// depends on it.
+__device__ uint32_t g_poh_round_warps[kMaxServeSms * 4];
+__device__ uint32_t g_poh_busy_slots;
+
+__device__ __forceinline__ uint32_t poh_place_enter() {
+    uint32_t smid, wid;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+    asm volatile("mov.u32 %0, %%warpid;" : "=r"(wid));
+    const uint32_t slot = ((smid % kMaxServeSms) << 2) | (wid & 3u);
+    if (atomicAdd(&g_poh_round_warps[slot], 1u) == 0u) atomicAdd(&g_poh_busy_slots, 1u);
+    return slot;
+}
+__device__ __forceinline__ void poh_place_leave(uint32_t slot) {
+    if (atomicSub(&g_poh_round_warps[slot], 1u) == 1u) atomicSub(&g_poh_busy_slots, 1u);
+}
+
 // BW independent warps per block.
 template <int BW>
 __global__ void __launch_bounds__(32 * BW) poh_persistent_kernel(uint8_t* hashes, const uint64_t* counts, uint32_t n,
                                                                  PohBatchScratch* s, uint32_t one) {
     const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t place = lane == 0 ? poh_place_enter() : 0u;
     uint32_t w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     uint64_t rem = 0;
     uint32_t cur = 0xffffffffu;
@@ -192,6 +216,7 @@ __global__ void __launch_bounds__(32 * BW) poh_persistent_kernel(uint8_t* hashes
             rem -= r;
         }
     }
+    if (lane == 0) poh_place_leave(place);
 }
 
 // Paired form: two warps per 32 lanes (the schedule warp computes the
@@ -389,11 +414,24 @@ __global__ void __launch_bounds__(64 * P) poh_pair_persistent_kernel(uint8_t* ha
     __shared__ uint64_t run_len[P];
     const uint32_t warp = threadIdx.x >> 5, pair = warp >> 1, role = warp & 1u;
     const uint32_t first = (blockIdx.x * P + pair) * 32u;   // direct mode only
+    const bool counted = role == 0 && (threadIdx.x & 31u) == 0;  // the round warp's place
+    const uint32_t place = counted ? poh_place_enter() : 0u;
     if (P == 1) pair_persistent<0>(hashes, counts, n, s, &run_len[0], role, 0, first, one);
     else pair_persistent<-1>(hashes, counts, n, s, &run_len[pair], role, pair, first, one);
+    if (counted) poh_place_leave(place);
 }
 
 }  // namespace
+
+cudaError_t poh_round_warp_map(const uint32_t** per_slot, const uint32_t** busy_slots) {
+    void* a = nullptr;
+    void* b = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&a, g_poh_round_warps);
+    if (e == cudaSuccess) e = cudaGetSymbolAddress(&b, g_poh_busy_slots);
+    *per_slot = static_cast<const uint32_t*>(a);
+    *busy_slots = static_cast<const uint32_t*>(b);
+    return e;
+}
 
 // The persistent PoH kernels run for up to seconds beside signature work.
 // An SM's split between L1 and shared memory is set for the blocks it holds;

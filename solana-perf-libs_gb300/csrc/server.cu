@@ -501,6 +501,7 @@ bool svc_create(gb300_server* sv) {
     V.params.idle_ns = 1000ull * (uint64_t)(idle && atoi(idle) > 0 ? atoi(idle) : 20000);
     V.params.tables = sv->info.tables;
     V.params.first_warps = 4u * (uint32_t)sv->info.sms;
+    if (poh_round_warp_map(&V.params.poh_slots, &V.params.poh_busy_slots) != cudaSuccess) return false;
     if (const char* b = getenv("GB300_CRYPT_SERVER_SVC_BLOCKS")) V.blocks_per_sm = atoi(b) > 0 ? atoi(b) : 2;
     void* fn = nullptr;
     cudaDriverEntryPointQueryResult q;

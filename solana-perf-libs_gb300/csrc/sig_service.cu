@@ -109,24 +109,28 @@ __device__ __forceinline__ S ld_volatile_struct(const S* p) {
 // with ~20 active threads and 2.6 branch-resolution stalls per issue, and
 // eight signatures took 3.0 ms against 0.46 ms in a plain launch.
 __device__ __forceinline__ bool claim_chunk(const SvcParams& p, uint32_t lane, uint32_t& c, uint64_t t_start,
-                                            bool first) {
+                                            bool first, uint32_t slot, bool& preferred) {
     uint32_t sleep_ns = 256;
     for (;;) {
-        uint32_t r = 3, got = 0;      // 0 leave, 1 claimed, 2 lost a race (look again), 3 empty
+        uint32_t r = 3, got = 0;      // 0 leave, 1 claimed (4: by a preferred warp), 2 lost a race, 3 empty
         if (lane == 0) {
             if (ld_relaxed_gpu(&p.dev->exiting)) {
                 r = 0;
             } else {
                 const uint32_t t = ld_relaxed_gpu(&p.dev->tail);
                 const uint32_t h = ld_relaxed_gpu(&p.dev->head);
-                // a warp of an SM's second block takes a chunk only when the
-                // waiting chunks outnumber the idle first-block warps
+                // preferred: a first-block warp on a sub-partition without
+                // a PoH round warp.  Any other warp takes a chunk only when
+                // the waiting chunks outnumber the idle preferred warps.
                 const int32_t waiting = (int32_t)(t - h);
+                const bool pref = first && ld_relaxed_gpu(p.poh_slots + slot) == 0u;
+                const int32_t n_pref = (int32_t)p.first_warps - (int32_t)ld_relaxed_gpu(p.poh_busy_slots);
                 const bool mine = waiting > 0 &&
-                                  (first || waiting > (int32_t)(p.first_warps - ld_relaxed_gpu(&p.dev->busy_first)));
+                                  (pref || waiting > n_pref - (int32_t)ld_relaxed_gpu(&p.dev->busy_first));
+                got = pref ? 1u : 0u;                    // (the chunk index replaces it on a claim)
                 if (mine) {
                     if (atomicCAS(&p.dev->head, h, h + 1u) == h) {
-                        r = 1;
+                        r = pref ? 4u : 1u;
                         got = h;
                         atomicMax(reinterpret_cast<unsigned long long*>(&p.dev->last_claim_ns),
                                   (unsigned long long)global_ns());
@@ -146,8 +150,9 @@ __device__ __forceinline__ bool claim_chunk(const SvcParams& p, uint32_t lane, u
         }
         r = __shfl_sync(0xffffffffu, r, 0);
         if (r == 0) return false;
-        if (r == 1) {
+        if (r == 1 || r == 4) {
             c = __shfl_sync(0xffffffffu, got, 0);
+            preferred = r == 4;
             return true;
         }
         if (r == 3) {
@@ -185,14 +190,23 @@ __global__ void __maxnreg__(216) sig_service_kernel(SvcParams p) {
     // warps take chunks first, so that a few chunks spread over the SMs'
     // sub-partitions instead of doubling up on some while others idle (a
     // verify chain is latency-bound: a second warp on the same
-    // sub-partition slows both).
+    // sub-partition slows both), and among them those whose sub-partition
+    // runs no PoH round warp.
     const bool first = s_rank == 0;
+    uint32_t slot;
+    {
+        uint32_t smid, wid;
+        asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+        asm volatile("mov.u32 %0, %%warpid;" : "=r"(wid));
+        slot = ((smid % kMaxServeSms) << 2) | (wid & 3u);  // as the PoH kernels count it
+    }
     const uint64_t t_start = global_ns();
     if (lane == 0) atomicAdd(&p.dev->warps, 1u);
     for (;;) {
         uint32_t c = 0;
-        if (!claim_chunk(p, lane, c, t_start, first)) break;
-        if (first && lane == 0) atomicAdd(&p.dev->busy_first, 1u);
+        bool preferred = false;
+        if (!claim_chunk(p, lane, c, t_start, first, slot, preferred)) break;
+        if (preferred && lane == 0) atomicAdd(&p.dev->busy_first, 1u);
         // every lane synchronises with the publication of chunk c (the
         // stream write of tail after the input copies): its later loads of
         // the descriptors (host memory) and inputs (device memory) see them
@@ -220,7 +234,7 @@ __global__ void __maxnreg__(216) sig_service_kernel(SvcParams p) {
             const bool ok = verify_window<W>(b, sVB, i);
             if (lane < ch.count) b.out[i] = ok ? 1 : 0;
         }
-        if (first && lane == 0) atomicSub(&p.dev->busy_first, 1u);
+        if (preferred && lane == 0) atomicSub(&p.dev->busy_first, 1u);
         // results (host memory) before the count; the completing warp
         // resets the slot's counter, then publishes the completion word
         __threadfence_system();
