@@ -127,7 +127,6 @@ __device__ __forceinline__ bool claim_chunk(const SvcParams& p, uint32_t lane, u
                 const int32_t n_pref = (int32_t)p.first_warps - (int32_t)ld_relaxed_gpu(p.poh_busy_slots);
                 const bool mine = waiting > 0 &&
                                   (pref || waiting > n_pref - (int32_t)ld_relaxed_gpu(&p.dev->busy_first));
-                got = pref ? 1u : 0u;                    // (the chunk index replaces it on a claim)
                 if (mine) {
                     if (atomicCAS(&p.dev->head, h, h + 1u) == h) {
                         r = pref ? 4u : 1u;
