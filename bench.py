@@ -799,6 +799,65 @@ def _pct(xs, q):
     return float(np.percentile(np.asarray(xs), q)) if len(xs) else None
 
 
+def fluid_latencies(arrivals, sizes, rate, policy="fifo"):
+    """Latencies (s) of requests into an ideal server: one fluid queue that
+    works at `rate` items/s whenever it holds work, with no per-request
+    minimum time.  "fifo" serves requests in arrival order; "srpt" always
+    serves the one with the least remaining work, preempting (the policy
+    with the lowest mean latency).  Any server whose throughput on this
+    stream is at most `rate` and which keeps the policy's order has
+    latencies at least these; a real GPU adds each request's minimum
+    latency (one signature's dependent chain)."""
+    n = len(arrivals)
+    lat = [0.0] * n
+    if policy == "fifo":
+        t = 0.0
+        for i, (a, s) in enumerate(zip(arrivals, sizes)):
+            t = max(t, a) + s / rate
+            lat[i] = t - a
+        return lat
+    import heapq
+    heap, t, i = [], 0.0, 0
+    while i < n or heap:
+        if not heap:
+            t = max(t, arrivals[i])
+        while i < n and arrivals[i] <= t:
+            heapq.heappush(heap, (sizes[i] / rate, i))
+            i += 1
+        rem, j = heapq.heappop(heap)
+        nxt = arrivals[i] if i < n else float("inf")
+        if t + rem <= nxt:
+            t += rem
+            lat[j] = t - arrivals[j]
+        else:
+            heapq.heappush(heap, (rem - (nxt - t), j))
+            t = nxt
+    return lat
+
+
+def fluid_max_load(sizes, rate, target_s=2e-3, q=99, n=4000, seed=19):
+    """Highest offered signature load (fraction of `rate`) at which the ideal
+    server of fluid_latencies keeps the q-th percentile latency within
+    target_s, for Poisson arrivals of requests drawn uniformly from `sizes`
+    (one seeded stream per load, bisection), per policy."""
+    sizes = np.asarray(sizes, dtype=np.float64)
+    out = {}
+    for policy in ("fifo", "srpt"):
+        lo, hi = 0.0, 1.0
+        for _ in range(12):
+            mid = 0.5 * (lo + hi)
+            rng = np.random.default_rng(seed)
+            lam = mid * rate / sizes.mean()
+            arr = np.cumsum(rng.exponential(1.0 / lam, n))
+            sz = sizes[rng.integers(0, len(sizes), n)]
+            if np.percentile(fluid_latencies(arr, sz, rate, policy), q) <= target_s:
+                lo = mid
+            else:
+                hi = mid
+        out[policy] = round(lo, 3)
+    return out
+
+
 def bench_serving(lib, levels=(0.1, 0.25, 0.5, 0.8, 1.0, 1.2), duration_s=1.0, max_requests=2500,
                   plain_requests=120, burst_n=1000, server_kwargs=None):
     """Open-loop Poisson arrivals of a request mix (80% verify batches of the
@@ -938,6 +997,16 @@ def bench_serving(lib, levels=(0.1, 0.25, 0.5, 0.8, 1.0, 1.2), duration_s=1.0, m
                     buckets[f"{lo}-{hi if hi < (1 << 30) else 'max'}"] = {
                         "share": len(xs) / len(by_size), "p50_ms": _pct(xs, 50) * 1e3, "p99_ms": _pct(xs, 99) * 1e3}
             row["sig_latency_by_size"] = buckets
+            # the same arrivals into an ideal server at the measured peak
+            # item rate: the floor any scheduler of that throughput faces
+            sig_arr = [ta for (kind, _), ta in zip(reqs, arrivals) if kind != "p"]
+            sig_sz = [items(kind, k) for kind, k in reqs if kind != "p"]
+            if sig_arr:
+                ideal = {}
+                for policy in ("fifo", "srpt"):
+                    xs = fluid_latencies(sig_arr, sig_sz, peak_items, policy)
+                    ideal[policy] = {"p50": _pct(xs, 50) * 1e3, "p99": _pct(xs, 99) * 1e3}
+                row["ideal_server_ms"] = ideal
             # resident signature service: where each request's time went on
             # the GPU (publication to first claimed chunk, then to completion)
             svc = [e for e in srv.trace() if e[0] == 4][-len(sig_lat):] if sig_lat else []
@@ -950,12 +1019,20 @@ def bench_serving(lib, levels=(0.1, 0.25, 0.5, 0.8, 1.0, 1.2), duration_s=1.0, m
         stats = srv.stats()
     finally:
         srv.close()
+    # signature requests of the mix (verify 80 : sign 5, pools of equal size)
+    mix_sizes = [sp.total_signatures for sp in vpool] * 16 + [sp.total_signatures for sp in spool]
+    ideal_note = {"rate_items_per_s": peak_items,
+                  "max_load_for_p99_2ms": fluid_max_load(mix_sizes, peak_items),
+                  "note": "each level's ideal_server_ms: the level's own signature arrivals into one fluid "
+                          "queue at the measured peak item rate (fifo: arrival order, srpt: least remaining "
+                          "work first); max_load_for_p99_2ms: the highest fraction of that rate at which such "
+                          "a server keeps p99 <= 2 ms for this mix's request sizes (Poisson, 4000 requests)"}
     if plain_requests <= 0:
         for sp in vpool + spool:
             for b in sp.batches:
                 lib.host_unregister(b)
         return {"peak_requests_per_s": peak_rps, "peak_sig_items_per_s": peak_items, "levels": rows,
-                "verify_request_alone_ms": alone_ms,
+                "verify_request_alone_ms": alone_ms, "ideal_server": ideal_note,
                 "results_identical_alone_and_in_mix": bool(ok_all), "alone_equals_oracle": oracle_ok,
                 "server_stats": stats}
     # the plain per-request calls at 80% of the served peak, 4 caller threads
@@ -1006,7 +1083,7 @@ def bench_serving(lib, levels=(0.1, 0.25, 0.5, 0.8, 1.0, 1.2), duration_s=1.0, m
                        "device_memory_cap_bytes": 8 << 30, "request_pool": {"verify": len(vpool), "sign": len(spool),
                                                                            "poh": len(ppool)}},
             "peak_requests_per_s": peak_rps, "peak_sig_items_per_s": peak_items, "levels": rows,
-            "verify_request_alone_ms": alone_ms,
+            "verify_request_alone_ms": alone_ms, "ideal_server": ideal_note,
             "p99_floor_note": "verify requests are drawn uniformly from the pool, so the largest one (of "
                               f"{len(vpool)}) is ~2% of the signature requests: the p99 cannot fall below its "
                               "latency alone (the last pair of verify_request_alone_ms: [signatures, ms])",
@@ -1251,6 +1328,11 @@ def summarize(line: dict) -> dict:
         if lv8 and lv8.get("sig_latency_by_size"):
             out["serving_mix"]["p99_ms_by_size_at_0.8"] = {k: r(v["p99_ms"], 3)
                                                            for k, v in lv8["sig_latency_by_size"].items()}
+        if lv8 and lv8.get("ideal_server_ms"):
+            out["serving_mix"]["ideal_server_p99_ms_at_0.8"] = {k: r(v["p99"], 3)
+                                                                for k, v in lv8["ideal_server_ms"].items()}
+        if sv.get("ideal_server"):
+            out["serving_mix"]["ideal_server_max_load_for_p99_2ms"] = sv["ideal_server"]["max_load_for_p99_2ms"]
         if sv.get("verify_request_alone_ms"):
             big = sv["verify_request_alone_ms"][-1]
             out["serving_mix"]["largest_verify_request_alone"] = {"signatures": big[0], "ms": r(big[1], 3)}
