@@ -741,17 +741,19 @@ def _served_packets(lib, w, out, counts, batch=128, levels=(0.25, 0.5, 0.8), max
     rng = np.random.default_rng(21)
     srv = Server(lib)
     try:
-        bursts = []
+        bursts, submits = [], []
         for rep in range(reps + 1):                   # the first burst warms the server up
             o, c, ob, cb = outputs(nb)
             t0 = time.perf_counter()
             tk = [submit(srv.h, run_addr[k], 1, stride, lens_addr[k], ob + k * batch, cb + 4 * k * batch)
                   for k in range(nb)]
+            t_sub = time.perf_counter() - t0
             for k, t in enumerate(tk):
                 assert t and srv.wait(t) == 1
                 ok &= same(k, o[k], c[k])
             if rep:
                 bursts.append(time.perf_counter() - t0)
+                submits.append(t_sub)
         burst_s = float(np.median(bursts))
         peak = nb / burst_s
         rows = []
@@ -789,7 +791,7 @@ def _served_packets(lib, w, out, counts, batch=128, levels=(0.25, 0.5, 0.8), max
         ok &= same(k, o, c)
     percall_s = time.perf_counter() - t0
     return {"workload": f"{nb} batches of {batch} packets", "peak_packets_per_s": nb * batch / burst_s,
-            "burst_s": burst_s, "levels": rows,
+            "burst_s": burst_s, "burst_submit_s": float(np.median(submits)), "levels": rows,
             "per_call_one_thread": {"packets_per_s": nb * batch / percall_s, "s": percall_s,
                                     "latency_ms_per_batch": percall_s / nb * 1e3},
             "results_identical": bool(ok), "server_stats": stats}
