@@ -80,8 +80,18 @@ enum PohBatchForm : int {
     kPohAuto = 5,           // kPohPair or kPohSingle (16 x SMs warps), chosen on the device from the counts
 };
 size_t poh_batch_workspace_size(uint64_t n);
+// A served-loop PoH launch that gives way to signature work (kPohPair only):
+// every 128 hashes its round warps read the signature service's FIFO and,
+// while at least `chunks` published chunks wait unclaimed, sleep (bounded),
+// leaving their SM sub-partitions to the service's warps.  A chain's result
+// does not depend on when it runs.
+struct PohYield {
+    const uint32_t* head;    // SvcDevice::head, device memory
+    const uint32_t* tail;    // SvcDevice::tail
+    uint32_t chunks;         // 0: never
+};
 cudaError_t launch_poh_batch(uint8_t* hashes, const uint64_t* counts, uint64_t n, void* workspace, int warps,
-                             cudaStream_t s, int form = kPohSingle);
+                             cudaStream_t s, int form = kPohSingle, const PohYield* yield = nullptr);
 // The direct paired form alone: poh_pair_persistent_kernel without a queue,
 // one block of two warps per 32 consecutive entries.
 cudaError_t launch_poh_pair_direct(uint8_t* hashes, const uint64_t* counts, uint64_t n, cudaStream_t s);

@@ -234,6 +234,38 @@ __global__ void __launch_bounds__(32 * BW) poh_persistent_kernel(uint8_t* hashes
 constexpr int kMaxPairsPerBlock = 2;
 __shared__ uint32_t pair_kw[kMaxPairsPerBlock][48][32];   // K[t] + W[t], t = 16..63, per lane
 __shared__ uint32_t pair_hout[kMaxPairsPerBlock][8][32];  // hash words, round warp -> schedule warp
+__shared__ PohYield pair_yield;                           // poh_pair_yield_kernel's hint, set at its start
+
+__device__ __forceinline__ uint32_t poh_ld_relaxed(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Published signature chunks not yet claimed (head read first: head never
+// passes the tail it was claimed under, so the difference is never negative).
+__device__ __forceinline__ uint32_t poh_sig_backlog() {
+    const uint32_t h = poh_ld_relaxed(pair_yield.head);
+    return poh_ld_relaxed(pair_yield.tail) - h;
+}
+
+// Hashes the yielding form runs between looks at the backlog (~115 us).
+constexpr uint64_t kYieldRun = 128;
+
+// The round warp (every lane, converged) sleeps while the backlog stays at
+// or above the threshold, its schedule warp waiting at the pair's barrier:
+// at most kYieldNaps naps of ~16 us, then it runs kYieldRun hashes before it
+// looks again.  The cap keeps PoH going under a backlog that lasts: with 256
+// naps (~4 ms) PoH nearly stopped at 100 % of the served mix's peak, fell
+// behind, and the signature p99 there doubled.
+constexpr int kYieldNaps = 32;
+__device__ __forceinline__ void poh_give_way() {
+#pragma unroll 1
+    for (int i = 0; i < kYieldNaps; i++) {
+        if (poh_sig_backlog() < pair_yield.chunks) break;
+        __nanosleep(16000);
+    }
+}
 
 __device__ __forceinline__ uint32_t sched_s0(uint32_t x) { return POH_ROTR(x, 7) ^ POH_ROTR(x, 18) ^ (x >> 3); }
 __device__ __forceinline__ uint32_t sched_s1(uint32_t x) { return POH_ROTR(x, 17) ^ POH_ROTR(x, 19) ^ (x >> 10); }
@@ -340,7 +372,7 @@ static __device__ __noinline__ void pair_schedule(HashWords in, uint32_t lane, u
 
 // s == nullptr: direct mode, no queue; the pair takes entries 32g .. 32g + 31
 // once (g = its index in the grid), in the order given.
-template <int PI>
+template <int PI, bool Y = false>
 __device__ __forceinline__ void pair_persistent(uint8_t* hashes, const uint64_t* counts, uint32_t n,
                                                 PohBatchScratch* s, uint64_t* run_len, uint32_t role, uint32_t pi,
                                                 uint32_t direct_first, uint32_t one) {
@@ -387,6 +419,13 @@ __device__ __forceinline__ void pair_persistent(uint8_t* hashes, const uint64_t*
                 r = other < r ? other : r;
             }
             if (r == ~0ull) r = 0;
+            if (Y && r > 0) {
+                // the yielding form runs at most kYieldRun hashes between
+                // looks at the signature backlog (the hashing loops stay
+                // those of the plain form)
+                if (r > kYieldRun) r = kYieldRun;
+                if (poh_sig_backlog() >= pair_yield.chunks) poh_give_way();
+            }
 #pragma unroll
             for (int t = 0; t < 8; t++) pair_hout[PAIR_IDX][t][lane] = w.v[t];
             if (lane == 0) *run_len = r;
@@ -421,6 +460,19 @@ __global__ void __launch_bounds__(64 * P) poh_pair_persistent_kernel(uint8_t* ha
     if (counted) poh_place_leave(place);
 }
 
+// The paired queue form that gives way to the signature service (PohYield).
+__global__ void __launch_bounds__(64) poh_pair_yield_kernel(uint8_t* hashes, const uint64_t* counts, uint32_t n,
+                                                            PohBatchScratch* s, uint32_t one, PohYield y) {
+    __shared__ uint64_t run_len;
+    if (threadIdx.x == 0) pair_yield = y;
+    __syncthreads();
+    const uint32_t role = threadIdx.x >> 5;
+    const bool counted = role == 0 && (threadIdx.x & 31u) == 0;
+    const uint32_t place = counted ? poh_place_enter() : 0u;
+    pair_persistent<0, true>(hashes, counts, n, s, &run_len, role, 0, 0, one);
+    if (counted) poh_place_leave(place);
+}
+
 }  // namespace
 
 cudaError_t poh_round_warp_map(const uint32_t** per_slot, const uint32_t** busy_slots) {
@@ -444,7 +496,7 @@ cudaError_t poh_round_warp_map(const uint32_t** per_slot, const uint32_t** busy_
 cudaError_t preload_poh_batch_kernels() {
     cudaError_t e = load_kernels(poh_hist_kernel, poh_scan_kernel, poh_scatter_kernel, poh_choose_kernel,
                                  poh_requeue_kernel, poh_persistent_kernel<1>, poh_persistent_kernel<4>,
-                                 poh_pair_persistent_kernel<1>, poh_pair_persistent_kernel<2>);
+                                 poh_pair_persistent_kernel<1>, poh_pair_persistent_kernel<2>, poh_pair_yield_kernel);
     const int pref = kServeCarveoutPercent;
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(poh_persistent_kernel<1>, cudaFuncAttributePreferredSharedMemoryCarveout, pref);
@@ -454,6 +506,8 @@ cudaError_t preload_poh_batch_kernels() {
         e = cudaFuncSetAttribute(poh_pair_persistent_kernel<1>, cudaFuncAttributePreferredSharedMemoryCarveout, pref);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(poh_pair_persistent_kernel<2>, cudaFuncAttributePreferredSharedMemoryCarveout, pref);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(poh_pair_yield_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pref);
     return e;
 }
 
@@ -468,7 +522,7 @@ cudaError_t launch_poh_pair_direct(uint8_t* hashes, const uint64_t* counts, uint
 }
 
 cudaError_t launch_poh_batch(uint8_t* hashes, const uint64_t* counts, uint64_t n, void* workspace,
-                             int warps, cudaStream_t s, int form) {
+                             int warps, cudaStream_t s, int form, const PohYield* yield) {
     if (n == 0) return cudaSuccess;
     if (n > 0xffffffffull) return cudaErrorInvalidValue;
     if (form == kPohPairDirect) return launch_poh_pair_direct(hashes, counts, n, s);
@@ -506,7 +560,10 @@ cudaError_t launch_poh_batch(uint8_t* hashes, const uint64_t* counts, uint64_t n
             poh_persistent_kernel<4><<<(unsigned)((nwarps + 3) / 4), 128, 0, s>>>(hashes, counts, (uint32_t)n, sc, 1u);
             break;
         case kPohPair:
-            poh_pair_persistent_kernel<1><<<(unsigned)pairs, 64, 0, s>>>(hashes, counts, (uint32_t)n, sc, 1u);
+            if (yield && yield->chunks && yield->head && yield->tail)
+                poh_pair_yield_kernel<<<(unsigned)pairs, 64, 0, s>>>(hashes, counts, (uint32_t)n, sc, 1u, *yield);
+            else
+                poh_pair_persistent_kernel<1><<<(unsigned)pairs, 64, 0, s>>>(hashes, counts, (uint32_t)n, sc, 1u);
             break;
         case kPohPackedPair:
             poh_pair_persistent_kernel<2><<<(unsigned)((pairs + 1) / 2), 128, 0, s>>>(hashes, counts, (uint32_t)n, sc,

@@ -111,6 +111,7 @@ constexpr uint32_t kSvcRing = 1u << 18;            // chunk descriptors (4 MiB)
 constexpr uint64_t kSvcStageBytes = 256ull << 20;  // page-locked staging: index arrays, pageable packets
 constexpr uint64_t kSvcResultBytes = 64ull << 20;  // page-locked results the GPU writes
 constexpr uint64_t kSvcDevBytes = 1ull << 30;      // device input ring (at most the memory cap)
+constexpr uint32_t kPohYieldChunks = 64;           // PoH gives way at this many waiting chunks (0: never)
 
 typedef CUresult (*WriteValue32Fn)(CUstream, CUdeviceptr, cuuint32_t, unsigned int);
 
@@ -174,6 +175,7 @@ struct gb300_server {
     uint64_t cap = 0, in_use = 0;
     uint32_t max_items = 0;
     int poh_form = kPohPackedSingle, poh_warps = 0;   // shape of the PoH launches
+    PohYield poh_yield{};                               // with the signature service: its FIFO
     std::vector<Slot> sig_slots, poh_slots;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
@@ -373,7 +375,7 @@ cudaError_t launch_pohs(gb300_server* sv, Slot& S) {
     if ((e = cudaMemcpyAsync(d, st, hb + cb, cudaMemcpyHostToDevice, S.stream)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(S.ev_run, S.stream)) != cudaSuccess) return e;
     if ((e = launch_poh_batch(d, reinterpret_cast<const uint64_t*>(d + hb), n, S.d_scratch.p, sv->poh_warps,
-                              S.stream, sv->poh_form)) != cudaSuccess)
+                              S.stream, sv->poh_form, sv->poh_yield.chunks ? &sv->poh_yield : nullptr)) != cudaSuccess)
         return e;
     if ((e = cudaEventRecord(S.ev_out, S.stream)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(st, d, hb, cudaMemcpyDeviceToHost, S.stream)) != cudaSuccess) return e;
@@ -503,6 +505,11 @@ bool svc_create(gb300_server* sv) {
     V.params.first_warps = 4u * (uint32_t)sv->info.sms;
     if (poh_round_warp_map(&V.params.poh_slots, &V.params.poh_busy_slots) != cudaSuccess) return false;
     if (const char* b = getenv("GB300_CRYPT_SERVER_SVC_BLOCKS")) V.blocks_per_sm = atoi(b) > 0 ? atoi(b) : 2;
+    // PoH launches give way while this many chunks wait unclaimed (PohYield)
+    sv->poh_yield.head = &V.d_state->head;
+    sv->poh_yield.tail = &V.d_state->tail;
+    sv->poh_yield.chunks = kPohYieldChunks;
+    if (const char* y = getenv("GB300_CRYPT_SERVER_POH_YIELD")) sv->poh_yield.chunks = (uint32_t)std::max(0, atoi(y));
     void* fn = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuStreamWriteValue32", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&

@@ -286,3 +286,32 @@ def test_service_mixed_order_keys(lib, oracle):
             assert srv.wait(t, 60000) == 1 and np.array_equal(out, exp)
     finally:
         srv.close()
+
+
+def test_service_poh_gives_way_to_a_signature_backlog(lib, oracle):
+    """PoH launches of the served loop sleep while signature chunks wait
+    unclaimed (threshold 1 chunk here): a PoH batch on every pair, then
+    three verify jobs of 20,000 signatures that queue more chunks than the
+    service has warps.  Every signature verdict is the oracle's and every
+    final PoH hash the plain call's (and the oracle's, on a sample)."""
+    sp, _ = workloads.verify_uniform(oracle.create_keypairs, oracle.sign_packets, n=20000, msg_len=64, seed=77)
+    exp = oracle.verify_packets(sp, nthreads())
+    ph, pc = workloads.poh_uniform(4864, 20000, seed=78)
+    plain = ph.ravel().copy()
+    assert lib.poh_verify_many(plain, pc) == 0
+    sample = np.arange(0, 4864, 76)
+    assert np.array_equal(plain.reshape(-1, 32)[sample], oracle.poh_verify_many(ph[sample], pc[sample], nthreads()))
+    with _env(GB300_CRYPT_SERVER_POH_YIELD=1):
+        srv = Server(lib)
+    try:
+        for rnd in range(2):
+            out = ph.ravel().copy()
+            tp = srv.submit_poh(out, pc)
+            time.sleep(0.005)
+            sub = [srv.submit_sigs(sp, JOB_VERIFY) for _ in range(3)]
+            for t, o in sub:
+                assert t and srv.wait(t, 60000) == 1 and np.array_equal(o, exp), rnd
+            assert tp and srv.wait(tp, 60000) == 1
+            assert np.array_equal(out, plain), rnd
+    finally:
+        srv.close()
