@@ -978,10 +978,14 @@ void gb300_server_destroy(gb300_server* sv) {
     int prev = -1;
     cudaGetDevice(&prev);
     cudaSetDevice(sv->dev);
+    // PoH launches read the service's FIFO words (PohYield): every slot's
+    // work ends before the service state is freed
+    for (auto* slots : {&sv->sig_slots, &sv->poh_slots})
+        for (auto& S : *slots)
+            if (S.stream) cudaStreamSynchronize(S.stream);
     svc_destroy(sv);
     for (auto* slots : {&sv->sig_slots, &sv->poh_slots})
         for (auto& S : *slots) {
-            if (S.stream) cudaStreamSynchronize(S.stream);
             S.d_data.release();
             S.d_index.release();
             S.d_out.release();
