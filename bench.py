@@ -1266,12 +1266,15 @@ def run_ours(args):
                                 "sample": f"8192 signs of 64-B messages on {nthreads} threads, CPU oracle"}
     line["ed25519_verify"] = verify
     line["ed25519_sign"] = sign
-    if not args.skip_ragged:
+    # the sections below describe one GPU; replicas (N > 1) time the headline only
+    if world > 1:
+        line["sections_at_n1_only"] = ["poh_ragged", "ragged_sigs", "wire_packets", "poh_entries", "serving"]
+    if not args.skip_ragged and world == 1:
         line["poh_ragged"] = bench_poh_ragged(lib, torch, steps=2)
         line["ragged_sigs"] = bench_ragged_sigs(lib, torch)
         line["wire_packets"] = bench_wire_packets(lib, torch, nthreads)
         line["poh_entries"] = bench_poh_entries(lib, torch, nthreads)
-    if not args.skip_serving:
+    if not args.skip_serving and world == 1:
         line["serving"] = bench_serving(lib)
         # the same mix with verify/sign jobs merged into slot launches instead
         # of the resident signature service, at 80 % of that form's own peak
