@@ -1468,6 +1468,10 @@ def run_case(case: str):
             lib.verify_device_form(pk, *arrs, out, lib.VERIFY_SINGLE, stream.cuda_stream)
     elif case == "sign-small":
         bench_sign_device(lib, torch, 152 * 64, reps=2)
+    elif case == "sign-big":         # the bench's signing launch (one inversion per block)
+        bench_sign_device(lib, torch, VERIFY_BIG_N, reps=1)
+    elif case == "sign-shared-min":  # the smallest launch that shares the inversion per block
+        bench_sign_device(lib, torch, 80000, reps=1)
     elif case in ("verify-1024-single", "verify-1024-quad", "verify-1024-trio"):
         sp, _ = make_verify_data(lib, 1024, seed=7)
         dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()

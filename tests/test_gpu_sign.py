@@ -93,3 +93,27 @@ def test_sign_device_form(lib, oracle):
     assert np.array_equal(out.cpu().numpy(), exp)
     epk, esk = oracle.create_keypairs(seeds.cpu().numpy())
     assert np.array_equal(dpk.cpu().numpy(), epk) and np.array_equal(dsk.cpu().numpy(), esk)
+
+
+def test_sign_many_shared_inversion(lib, oracle):
+    """From 80,000 signatures a launch shares one field inversion per block
+    (sign.cu): 82,000 signatures, the last block partial, equal the oracle's;
+    with a few items' offsets out of range, those signatures are zero and
+    every other one in their blocks is unchanged."""
+    rng = np.random.default_rng(55)
+    n = 82000
+    pk, sk = oracle.create_keypairs(rng.integers(0, 256, (n, 32), dtype=np.uint8))
+    lens = rng.integers(0, 65, n)
+    items = [(bytes(rng.integers(0, 256, int(lens[i]), dtype=np.uint8).tolist()), bytes(pk[i]),
+              bytes(sk[i]) if i % 7 else bytes(rng.integers(0, 256, 64, dtype=np.uint8).tolist()))
+             for i in range(n)]
+    sp = _sign_items(items)
+    got = lib.sign_many(sp)
+    assert np.array_equal(got, oracle.sign_packets(sp, nthreads()))
+    bad = np.array([5, 130, n - 1])
+    mso = sp.message_start_offsets.copy()
+    mso[bad] = len(sp.concatenated()) + 1
+    sp2 = SigPackets(sp.batches, sp.message_size, sp.message_lens, sp.public_key_offsets, sp.signature_offsets, mso)
+    got2 = lib.sign_many(sp2)
+    keep = np.setdiff1d(np.arange(n), bad)
+    assert not got2[bad].any() and np.array_equal(got2[keep], got[keep])
