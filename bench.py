@@ -859,7 +859,7 @@ def fluid_max_load(sizes, rate, target_s=2e-3, q=99, n=4000, seed=19):
     return out
 
 
-def bench_serving(lib, levels=(0.1, 0.25, 0.5, 0.8, 1.0, 1.2), duration_s=1.0, max_requests=2500,
+def bench_serving(lib, levels=(0.1, 0.25, 0.5, 0.8, 1.0, 1.2), duration_s=2.0, max_requests=10000,
                   plain_requests=120, burst_n=1000, server_kwargs=None):
     """Open-loop Poisson arrivals of a request mix (80% verify batches of the
     ragged-batch size/message/adversarial distributions, 15% PoH batches of

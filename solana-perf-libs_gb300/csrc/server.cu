@@ -112,6 +112,7 @@ constexpr uint64_t kSvcStageBytes = 256ull << 20;  // page-locked staging: index
 constexpr uint64_t kSvcResultBytes = 64ull << 20;  // page-locked results the GPU writes
 constexpr uint64_t kSvcDevBytes = 1ull << 30;      // device input ring (at most the memory cap)
 constexpr uint32_t kPohYieldChunks = 64;           // PoH gives way at this many waiting chunks (0: never)
+constexpr size_t kTraceCap = 16384;                // launch-trace entries kept (the oldest quarter goes when full)
 
 typedef CUresult (*WriteValue32Fn)(CUstream, CUdeviceptr, cuuint32_t, unsigned int);
 
@@ -749,7 +750,7 @@ void dispatcher(gb300_server* sv) {
                 auto it = sv->times.find(d.ticket);
                 if (it != sv->times.end()) {
                     it->second.second = d.t_done;
-                    if (sv->trace.size() >= 4096) sv->trace.erase(sv->trace.begin(), sv->trace.begin() + 1024);
+                    if (sv->trace.size() >= kTraceCap) sv->trace.erase(sv->trace.begin(), sv->trace.begin() + kTraceCap / 4);
                     sv->trace.push_back({4, 1u, d.n, it->second.first, d.t_pub, d.t_done, d.wait_ms, d.run_ms,
                                          (float)((d.t_done - d.t_pub) * 1e-6)});
                 }
@@ -785,7 +786,7 @@ void dispatcher(gb300_server* sv) {
                 {
                     uint64_t it = 0;
                     for (auto& r : S.reqs) it += r.n;
-                    if (sv->trace.size() >= 4096) sv->trace.erase(sv->trace.begin(), sv->trace.begin() + 1024);
+                    if (sv->trace.size() >= kTraceCap) sv->trace.erase(sv->trace.begin(), sv->trace.begin() + kTraceCap / 4);
                     float ms_in = -1.f, ms_run = -1.f, ms_out = -1.f;
                     if (S.err == cudaSuccess) {
                         if (cudaEventElapsedTime(&ms_in, S.ev_in, S.ev_run) != cudaSuccess) ms_in = -1.f;
