@@ -935,8 +935,40 @@ def bench_serving(lib, levels=(0.1, 0.25, 0.5, 0.8, 1.0, 1.2), duration_s=2.0, m
         for kind, k, t, out in subs:
             srv.wait(t)
             ok_all &= check(kind, k, out)
-        peak_rps = len(burst) / (last_sig - t0)
-        peak_items = sum(items(kd, k) for kd, k in burst) / (last_sig - t0)
+        burst_rps = len(burst) / (last_sig - t0)
+        burst_items = sum(items(kd, k) for kd, k in burst) / (last_sig - t0)
+        # The sustained peak: the mix offered open-loop at 1.5 x the burst's
+        # rate for 2 s.  A burst ends before the PoH work of its requests
+        # (~1.3 s each) reaches steady state, so it overstates what the loop
+        # carries beside steady PoH.  By the second half of this window the
+        # loop is saturated; the signature requests it completes there give
+        # the rate it sustains (signature requests are 85 % of the mix).
+        lam = 1.5 * burst_rps
+        m = min(16000, int(lam * 2.0))
+        arrivals = np.cumsum(rng.exponential(1.0 / lam, m))
+        reqs = draw(m)
+        start = time.perf_counter()
+        subs = []
+        for (kind, k), ta in zip(reqs, arrivals):
+            dt = start + ta - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            subs.append((kind, k) + tuple(submit(srv, kind, k)))
+        sig_done, sub_first, sub_last = [], None, None
+        for kind, k, t, out in subs:
+            srv.wait(t, release=False)
+            a, b = srv.times_ns(t)
+            sub_first = a if sub_first is None else min(sub_first, a)
+            sub_last = a if sub_last is None else max(sub_last, a)
+            if kind != "p":
+                sig_done.append((b, items(kind, k)))
+            ok_all &= check(kind, k, out)
+            srv.release(t)
+        w0 = sub_first + (sub_last - sub_first) // 2
+        span_s = max(1e-9, (sub_last - w0) * 1e-9)
+        in_window = [it for b, it in sig_done if w0 <= b <= sub_last]
+        peak_rps = len(in_window) / span_s / 0.85
+        peak_items = sum(in_window) / span_s
         # each verify request of the pool alone through the server (GPU idle
         # otherwise): the floor under any load
         alone_ms = []
@@ -1039,7 +1071,8 @@ def bench_serving(lib, levels=(0.1, 0.25, 0.5, 0.8, 1.0, 1.2), duration_s=2.0, m
         for sp in vpool + spool:
             for b in sp.batches:
                 lib.host_unregister(b)
-        return {"peak_requests_per_s": peak_rps, "peak_sig_items_per_s": peak_items, "levels": rows,
+        return {"peak_requests_per_s": peak_rps, "peak_sig_items_per_s": peak_items,
+                "burst_peak_requests_per_s": burst_rps, "burst_peak_sig_items_per_s": burst_items, "levels": rows,
                 "verify_request_alone_ms": alone_ms, "ideal_server": ideal_note,
                 "results_identical_alone_and_in_mix": bool(ok_all), "alone_equals_oracle": oracle_ok,
                 "server_stats": stats}
@@ -1090,7 +1123,12 @@ def bench_serving(lib, levels=(0.1, 0.25, 0.5, 0.8, 1.0, 1.2), duration_s=2.0, m
                                    "num_hashes log-uniform 1..1e6), 5% sign batches (128 packets)",
                        "device_memory_cap_bytes": 8 << 30, "request_pool": {"verify": len(vpool), "sign": len(spool),
                                                                            "poh": len(ppool)}},
-            "peak_requests_per_s": peak_rps, "peak_sig_items_per_s": peak_items, "levels": rows,
+            "peak_requests_per_s": peak_rps, "peak_sig_items_per_s": peak_items,
+            "burst_peak_requests_per_s": burst_rps, "burst_peak_sig_items_per_s": burst_items,
+            "peak_method": "sustained: the mix offered open-loop at 1.5 x a 1,000-request burst's rate for 2 s; "
+                           "signature requests completed in the window's second half (the loop saturated), "
+                           "over 0.85 (their share of the mix)",
+            "levels": rows,
             "verify_request_alone_ms": alone_ms, "ideal_server": ideal_note,
             "p99_floor_note": "verify requests are drawn uniformly from the pool, so the largest one (of "
                               f"{len(vpool)}) is ~2% of the signature requests: the p99 cannot fall below its "
@@ -1331,6 +1369,7 @@ def summarize(line: dict) -> dict:
     if "serving" in line:
         sv = line["serving"]
         out["serving_mix"] = {"peak_requests_per_s": r(sv["peak_requests_per_s"]),
+                              "burst_peak_requests_per_s": r(sv.get("burst_peak_requests_per_s")),
                               "sig_p50_ms": {str(x["offered_fraction_of_peak"]): r(x["sig_latency_ms"]["p50"], 3)
                                              for x in sv["levels"]},
                               "sig_p99_ms": {str(x["offered_fraction_of_peak"]): r(x["sig_latency_ms"]["p99"], 3)
