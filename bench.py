@@ -701,6 +701,32 @@ def bench_wire_packets(lib, torch, nthreads, n=16384, reps=5):
                              "sample": f"the full batch ({nsig} signatures), CPU oracle parse + verify"}}
 
 
+def _without_gc(fn):
+    """Runs fn with the interpreter's cyclic garbage collector off (one
+    collection first).  The served-loop sections submit requests from this
+    thread on a Poisson schedule, and hold tens of thousands of requests and
+    trace entries: a full collection paused the submitter for 15-35 ms, so
+    no request was published meanwhile and the delayed ones then arrived
+    together (a launch trace showed 35 ms without a publication, then
+    350 k signature items within 10 ms).  A native caller has no such
+    pauses; the library is what is measured."""
+    import functools
+    import gc
+
+    @functools.wraps(fn)
+    def run(*args, **kwargs):
+        gc.collect()
+        was_on = gc.isenabled()
+        gc.disable()
+        try:
+            return fn(*args, **kwargs)
+        finally:
+            if was_on:
+                gc.enable()
+    return run
+
+
+@_without_gc
 def _served_packets(lib, w, out, counts, batch=128, levels=(0.25, 0.5, 0.8), max_requests=4000, reps=3):
     """The same packets as a stream of `batch`-packet batches (views of the
     page-locked buffer) through the served loop
@@ -859,6 +885,7 @@ def fluid_max_load(sizes, rate, target_s=2e-3, q=99, n=4000, seed=19):
     return out
 
 
+@_without_gc
 def bench_serving(lib, levels=(0.1, 0.25, 0.5, 0.8, 1.0, 1.2), duration_s=2.0, max_requests=10000,
                   plain_requests=120, burst_n=1000, server_kwargs=None):
     """Open-loop Poisson arrivals of a request mix (80% verify batches of the
