@@ -1067,7 +1067,11 @@ def bench_serving(lib, levels=(0.1, 0.25, 0.5, 0.8, 1.0, 1.2), duration_s=2.0, m
                 row["service_gpu_ms"] = {"wait_p50": _pct([e[6] for e in svc], 50),
                                          "wait_p99": _pct([e[6] for e in svc], 99),
                                          "run_p50": _pct([e[7] for e in svc], 50),
-                                         "run_p99": _pct([e[7] for e in svc], 99)}
+                                         "run_p99": _pct([e[7] for e in svc], 99),
+                                         # host side: submission to publication (ring space,
+                                         # staging), and GPU completion to the host seeing it
+                                         "publish_p99": _pct([(e[4] - e[3]) * 1e-6 for e in svc], 99),
+                                         "detect_p99": _pct([e[8] - e[6] - e[7] for e in svc], 99)}
             rows.append(row)
         stats = srv.stats()
     finally:
