@@ -38,3 +38,21 @@ def test_max_load():
     assert bench.fluid_max_load([32] * 10, 16e6)["fifo"] > 0.95
     # requests that alone take longer than the target never meet it
     assert bench.fluid_max_load([64000] * 10, 16e6) == {"fifo": 0.0, "srpt": 0.0}
+
+
+def test_without_gc_restores_the_collector():
+    import gc
+
+    @bench._without_gc
+    def inside(fail=False):
+        if fail:
+            raise ValueError("x")
+        return gc.isenabled()
+
+    assert gc.isenabled()
+    assert inside() is False and gc.isenabled()
+    try:
+        inside(fail=True)
+    except ValueError:
+        pass
+    assert gc.isenabled()
