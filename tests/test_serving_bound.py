@@ -1,6 +1,7 @@
 """The ideal-server model the bench's serving section reports beside each
 load level (bench.fluid_latencies, bench.fluid_max_load): worked cases by
-hand, and the properties the bound relies on."""
+hand, and the properties the bound relies on; and the wrapper that keeps
+the garbage collector off while that section submits (bench._without_gc)."""
 import numpy as np
 
 import bench
